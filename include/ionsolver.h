@@ -1,0 +1,233 @@
+/*
+ * ionsolver.h -- C ABI of the GB300 (sm_103a) implementation of IonSolver's
+ * single-node MHD lattice-Boltzmann timestep.
+ *
+ * Every entry point replaces one call of the reference's Rust API for this
+ * path; the reference interface is cited beside each declaration as
+ * `file:line` inside the IonSolver crate (src/...).  Conventions:
+ *
+ *   - every function returns int: ION_OK (0) or a negative ION_E_* code;
+ *     ion_last_error() gives a message for the calling thread.  Nothing
+ *     aborts the process (the reference panics or exits instead).
+ *   - host arrays are caller-owned and copied; device memory is owned by the
+ *     handle.  Arrays use the reference's SoA layout: a cell index is
+ *     n = x + (y + z*n_y)*n_x, vectors are [3][N], DDFs are [q][N].
+ *   - one handle owns one CUDA stream and is not thread-safe; distinct
+ *     handles may be used from distinct threads.
+ */
+#ifndef IONSOLVER_H
+#define IONSOLVER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ION_ABI_VERSION 1
+
+/* ---- status codes ---------------------------------------------------- */
+#define ION_OK 0
+#define ION_E_INVALID   (-1)  /* bad argument / null pointer / wrong size   */
+#define ION_E_CONFIG    (-2)  /* configuration not supported by this build  */
+#define ION_E_CUDA      (-3)  /* CUDA runtime error                         */
+#define ION_E_NOMEM     (-4)  /* device or host allocation failed           */
+#define ION_E_IO        (-5)  /* file could not be opened / written         */
+#define ION_E_FORMAT    (-6)  /* file content malformed (header, size, ...) */
+#define ION_E_TIMEOUT   (-7)  /* bounded wait expired                       */
+#define ION_E_STATE     (-8)  /* call not valid in the handle's state       */
+
+/* ---- enums (values equal the reference's `as u8` casts) -------------- */
+/* VelocitySet, src/lbm/types.rs:16-26 */
+enum { ION_D2Q9 = 0, ION_D3Q15 = 1, ION_D3Q19 = 2, ION_D3Q27 = 3 };
+/* RelaxationTime, src/lbm/types.rs:55-61 */
+enum { ION_SRT = 0, ION_TRT = 1 };
+/* FloatType, src/lbm/types.rs:75-83 */
+enum { ION_FP16S = 0, ION_FP16C = 1, ION_FP32 = 2 };
+/* Propellant, src/lbm/units.rs:324-332 */
+enum { ION_PROP_H = 0, ION_PROP_HE, ION_PROP_NE, ION_PROP_AR, ION_PROP_KR, ION_PROP_XE };
+/* How the dynamic E/B far field is evaluated each step (no reference
+ * counterpart: the reference always runs update_e_b_dynamic,
+ * src/kernels/sim_kernels.cl:897-993).
+ *   BITWISE: the reference's summation order and IEEE operations, results
+ *            bit-identical to the reference kernel run in cell order;
+ *   FAST:    same sources and sum order, reciprocal-sqrt/FMA arithmetic;
+ *   SURROGATE: learned far field with a sampled exact check and fallback. */
+enum { ION_FIELD_BITWISE = 0, ION_FIELD_FAST = 1, ION_FIELD_SURROGATE = 2 };
+
+/* Field identifiers for read/write (the pub buffers of LbmDomain,
+ * src/lbm/domain.rs:45-74). */
+enum {
+    ION_FIELD_FI = 0,      /* DDFs, [q][N], f32 or u16 (float_type)        */
+    ION_FIELD_RHO = 1,     /* f32 [N]                                      */
+    ION_FIELD_U = 2,       /* f32 [3][N]                                   */
+    ION_FIELD_FLAGS = 3,   /* u8  [N]                                      */
+    ION_FIELD_F = 4,       /* f32 [3][N] force field (ext_force_field)     */
+    ION_FIELD_E_STAT = 5,  /* f32 [3][N]                                   */
+    ION_FIELD_B_STAT = 6,  /* f32 [3][N]                                   */
+    ION_FIELD_E_DYN = 7,   /* f32 [3][N] (or larger, see ion_lbm_field_info)*/
+    ION_FIELD_B_DYN = 8,   /* f32 [3][N]                                   */
+    ION_FIELD_FQI = 9,     /* charge DDFs, [7][N], f32 or u16              */
+    ION_FIELD_EI = 10,     /* electron-gas DDFs, [q][N], f32 or u16        */
+    ION_FIELD_Q = 11,      /* f32 [N] cell charge                          */
+    ION_FIELD_QU_LOD = 12, /* f32 [n_lod][4] charge + velocity LOD         */
+    ION_FIELD_COUNT = 13
+};
+
+/* ModelType -> flag byte, src/mesh.rs:9-14, 309-314 */
+enum { ION_MODEL_SOLID = 0, ION_MODEL_MAGNET = 1, ION_MODEL_CHARGED = 2, ION_MODEL_CHARGED_ECR = 3 };
+
+/* Units, src/lbm/units.rs:122-137 */
+typedef struct ion_units {
+    float m, kg, s, a, k;
+    int32_t prop;
+} ion_units;
+
+/* LbmConfig, src/lbm/mod.rs:45-101.  The graphics_config member is replaced
+ * by `update_fields`, its only effect on the timestep (graphics_active turns
+ * on UPDATE_FIELDS, src/lbm/domain.rs:856); `field_mode` is new. */
+typedef struct ion_config {
+    int32_t velocity_set;          /* ION_D2Q9 ... ION_D3Q27   */
+    int32_t relaxation_time;       /* ION_SRT / ION_TRT        */
+    int32_t float_type;            /* ION_FP16S/ION_FP16C/ION_FP32 */
+    ion_units units;
+    uint32_t n_x, n_y, n_z;
+    uint32_t d_x, d_y, d_z;        /* must be 1: one GPU, no decomposition */
+    float nu;
+    float f_x, f_y, f_z;
+    uint8_t ext_equilibrium_boundaries;
+    uint8_t ext_volume_force;
+    uint8_t ext_force_field;
+    uint8_t ext_magneto_hydro;
+    uint8_t ext_subgrid_ecr;       /* not supported: must be 0 */
+    uint8_t mhd_lod_depth;
+    uint8_t update_fields;
+    uint8_t field_mode;            /* ION_FIELD_*              */
+    float ecr_freq, ecr_field_strength;
+    uint64_t run_steps;
+} ion_config;
+
+/* Constants derived from Units that the kernels use
+ * (src/lbm/units.rs:145-177, 259-307; src/lbm/domain.rs:808, 838-848). */
+typedef struct ion_constants {
+    float w;        /* DEF_W   = 1/(3 nu + 1/2)            */
+    float ke;       /* DEF_KE  = ke_lu                     */
+    float kmu;      /* DEF_KMU = mu_0_lu / (4 pi)          */
+    float kmu0;     /* DEF_KMU0 = mu_0_lu                  */
+    float kkge;     /* DEF_KKGE = kkge_lu                  */
+    float kimg;     /* DEF_KIMG = kimg_lu                  */
+    float kvev;     /* DEF_KVEV = kveV_lu                  */
+    float kme;      /* DEF_KME  = kme_lu                   */
+    float wq;       /* DEF_WQ  = 1/(2 k_charge_expansion + 1/2) */
+    float epsilon_0;/* epsilon_0_lu                        */
+    float mu_0;     /* mu_0_lu                             */
+} ion_constants;
+
+typedef struct ion_lbm ion_lbm;   /* opaque: Lbm with its single LbmDomain */
+
+/* ---- library ---------------------------------------------------------- */
+int ion_abi_version(void);
+const char* ion_last_error(void);
+/* Number of CUDA kernel launches this process made through the library. */
+uint64_t ion_kernel_launch_count(void);
+
+/* LbmConfig::new(), src/lbm/mod.rs:105-135 */
+int ion_config_default(ion_config* cfg);
+/* Units::new(), src/lbm/units.rs:140-149 */
+int ion_units_default(ion_units* u);
+/* Units::set(...), src/lbm/units.rs:151-169 */
+int ion_units_set(ion_units* u, float lbm_length, float lbm_velocity, float lbm_rho,
+                  float lbm_charge, float lbm_temp, float si_length, float si_velocity,
+                  float si_rho, float si_charge, float si_temp);
+/* The kernel constants for a config (get_device_defines, src/lbm/domain.rs:736-858) */
+int ion_constants_from_config(const ion_config* cfg, ion_constants* out);
+/* Units::nu_si_lu / magnetization_si_lu / charge_si_lu / len_si_lu
+ * (src/lbm/units.rs:236-257, 212-214): what selects the conversion:
+ * 0 = nu, 1 = magnetization, 2 = charge, 3 = length. */
+int ion_units_si_to_lu(const ion_units* u, int what, float value, float* out);
+
+/* ---- lifecycle (Lbm::new, src/lbm/mod.rs:166-210; LbmDomain::new,
+ *      src/lbm/domain.rs:88-409) ------------------------------------------ */
+int ion_lbm_create(const ion_config* cfg, ion_lbm** out);
+int ion_lbm_destroy(ion_lbm* h);
+int ion_lbm_get_config(const ion_lbm* h, ion_config* out);
+
+/* ---- step loop -------------------------------------------------------- */
+/* Lbm::initialize, src/lbm/mod.rs:214-231 */
+int ion_lbm_initialize(ion_lbm* h);
+/* Lbm::do_time_step, src/lbm/mod.rs:250-272 (asynchronous on the handle's
+ * stream; the reference blocks in finish_queues, mod.rs:267-270) */
+int ion_lbm_do_time_step(ion_lbm* h);
+/* Lbm::run, src/lbm/mod.rs:235-245 (initializes first if needed; replays
+ * the step as a captured CUDA graph; asynchronous) */
+int ion_lbm_run(ion_lbm* h, uint64_t steps);
+/* Lbm::get_time_step, src/lbm/mod.rs:492-494 */
+int ion_lbm_get_time_step(const ion_lbm* h, uint64_t* t);
+/* Lbm::finish_queues, src/lbm/mod.rs:275-279, with a bound on the wait:
+ * returns ION_E_TIMEOUT if the stream is still busy after timeout_ms
+ * (timeout_ms < 0: wait without bound). */
+int ion_lbm_finish_queues(ion_lbm* h, int timeout_ms);
+/* LbmDomain::enqueue_update_fields, src/lbm/domain.rs:432-441 */
+int ion_lbm_update_fields(ion_lbm* h);
+
+/* ---- field access (bwrite!/bread! on the pub buffers, e.g.
+ *      src/setup.rs:180-184, src/file.rs:118-153, 233-269) --------------- */
+/* element size in bytes and element count of a field (0 if absent) */
+int ion_lbm_field_info(const ion_lbm* h, int field, size_t* elem_bytes, size_t* count);
+int ion_lbm_write_field(ion_lbm* h, int field, const void* host, size_t bytes);
+int ion_lbm_read_field(ion_lbm* h, int field, void* host, size_t bytes);
+/* device pointer of a field (valid until ion_lbm_destroy) */
+int ion_lbm_field_device_ptr(ion_lbm* h, int field, void** dptr, size_t* bytes);
+/* the handle's cudaStream_t */
+int ion_lbm_stream(ion_lbm* h, void** stream);
+
+/* ---- geometry (Lbm::import_mesh*, voxelise_mesh, precompute_B/E;
+ *      src/mesh.rs:233-343, src/lbm/mod.rs:284-314) ----------------------- */
+/* Adds a triangle mesh given in lattice coordinates; p0/p1/p2 are [ntri][3].
+ * The bounding box is computed as Mesh::update_bounds (src/mesh.rs:94-109). */
+int ion_lbm_add_mesh(ion_lbm* h, const float* p0, const float* p1, const float* p2,
+                     uint32_t ntri, uint32_t* index);
+/* Lbm::import_mesh, src/mesh.rs:233-239 (binary STL) */
+int ion_lbm_import_mesh(ion_lbm* h, const char* path, float scale, float ox, float oy, float oz,
+                        float rx, float ry, float rz, uint32_t* index);
+/* Lbm::import_mesh_reposition, src/mesh.rs:248-253 */
+int ion_lbm_import_mesh_reposition(ion_lbm* h, const char* path, float cx, float cy, float cz,
+                                   float rx, float ry, float rz, float size, uint32_t* index);
+/* Mesh::translate, src/mesh.rs:121-130 */
+int ion_lbm_mesh_translate(ion_lbm* h, uint32_t index, float dx, float dy, float dz);
+/* mesh bounds: out[0..2] = p_min, out[3..5] = p_max, out[6..8] = center */
+int ion_lbm_mesh_bounds(const ion_lbm* h, uint32_t index, float* out9);
+/* Lbm::voxelise_mesh(index, ModelType), src/mesh.rs:256-343.
+ * v0..v2 = magnetization (A/m, Magnet) or v0 = charge (C, Charged*). */
+int ion_lbm_voxelise_mesh(ion_lbm* h, uint32_t index, int model_type, float v0, float v1, float v2);
+/* Lbm::precompute_B, src/lbm/mod.rs:284-297 */
+int ion_lbm_precompute_b(ion_lbm* h);
+
+/* ---- FP64 domain reductions (no reference counterpart) ----------------- */
+/* sum of rho and of Q over non-solid cells, accumulated in double */
+int ion_lbm_mass_charge(ion_lbm* h, double* mass, double* charge);
+
+/* ---- persistence (file::write / file::read, src/file.rs:12-30, 42-306;
+ *      FILE_LAYOUT.txt) --------------------------------------------------- */
+int ion_lbm_save(ion_lbm* h, const char* path);
+/* Creates a handle from an .ion file; cfg_inout supplies the fields the file
+ * does not hold (as the reference's `config` argument does) and receives
+ * the decoded config. */
+int ion_lbm_load(const char* path, ion_config* cfg_inout, ion_lbm** out);
+
+/* ---- timing helpers on the handle's stream ---------------------------- */
+/* records a CUDA event on the handle's stream; slot 0..7 */
+int ion_lbm_record_event(ion_lbm* h, int slot);
+/* elapsed ms between two recorded slots (synchronizes on `end`) */
+int ion_lbm_event_elapsed(ion_lbm* h, int start, int end, float* ms);
+/* per-kernel timing: when enabled, every launch of the dominant kernels is
+ * bracketed by events; read back as total ms and launch count per kernel. */
+int ion_lbm_set_kernel_timing(ion_lbm* h, int enable);
+/* kernel: 0 = stream_collide, 1 = update_e_b, 2 = lod bins */
+int ion_lbm_kernel_time(ion_lbm* h, int kernel, double* total_ms, uint64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IONSOLVER_H */
