@@ -128,6 +128,14 @@ typedef struct ion_lbm ion_lbm;   /* opaque: Lbm with its single LbmDomain */
 
 /* ---- library ---------------------------------------------------------- */
 int ion_abi_version(void);
+/* cudaSetDevice for the calling thread (the reference picks devices in
+ * opencl::device_selection, src/opencl.rs:9-63); handles use the device that
+ * is current when they are created. */
+int ion_select_device(int device);
+/* Measured FP32 FMA throughput of the current device in TFLOP/s (FMA = 2
+ * FLOP; no reference counterpart): the roofline denominator of the
+ * FP32-bound field kernel. */
+int ion_probe_fp32_peak(double* tflops);
 const char* ion_last_error(void);
 /* Number of CUDA kernel launches this process made through the library. */
 uint64_t ion_kernel_launch_count(void);
@@ -203,6 +211,8 @@ int ion_lbm_mesh_bounds(const ion_lbm* h, uint32_t index, float* out9);
 int ion_lbm_voxelise_mesh(ion_lbm* h, uint32_t index, int model_type, float v0, float v1, float v2);
 /* Lbm::precompute_B, src/lbm/mod.rs:284-297 */
 int ion_lbm_precompute_b(ion_lbm* h);
+/* Lbm::precompute_E, src/lbm/mod.rs:302-314 (static E of charged solids) */
+int ion_lbm_precompute_e(ion_lbm* h);
 
 /* ---- FP64 domain reductions (no reference counterpart) ----------------- */
 /* sum of rho and of Q over non-solid cells, accumulated in double */
@@ -226,6 +236,14 @@ int ion_lbm_event_elapsed(ion_lbm* h, int start, int end, float* ms);
 int ion_lbm_set_kernel_timing(ion_lbm* h, int enable);
 /* kernel: 0 = stream_collide, 1 = update_e_b, 2 = lod bins */
 int ion_lbm_kernel_time(ion_lbm* h, int kernel, double* total_ms, uint64_t* launches);
+int ion_lbm_reset_kernel_time(ion_lbm* h);
+
+/* ---- storage codecs on the device (no reference counterpart; exposes the
+ *      FP16S/FP16C codecs of src/lbm/domain.rs:773-780 and
+ *      src/kernels/sim_kernels.cl:79-90 for exhaustive checks) ------------ */
+/* enc[i] = encode(in[i]), dec[i] = decode(enc[i]), raw_dec[i] = decode(raw[i]) */
+int ion_codec_roundtrip(int float_type, const float* in, uint16_t* enc, float* dec, const uint16_t* raw,
+                        float* raw_dec, uint64_t n);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,1052 @@
+// ion_api.cu -- the C ABI of include/ionsolver.h: a one-domain Lbm on one GPU.
+//
+// Host orchestration restated from IonSolver's Rust host
+// (src/lbm/mod.rs, src/lbm/domain.rs, src/mesh.rs, src/file.rs,
+// src/lbm/units.rs); kernels in lbm_q*.cu, field_kernels.cu,
+// setup_kernels.cu.  Nothing here computes physics on the CPU.
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "ion_device.cuh"
+#include "ion_launch.h"
+
+using namespace ion;
+
+namespace {
+
+thread_local std::string g_error;
+std::atomic<uint64_t> g_launches{0};
+
+int fail(int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_error = buf;
+    return code;
+}
+
+#define CK(call)                                                                                      \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess) return fail(ION_E_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                                           __FILE__, __LINE__);                                       \
+    } while (0)
+
+#define CKL()                                                                                         \
+    do {                                                                                              \
+        cudaError_t e_ = cudaGetLastError();                                                          \
+        if (e_ != cudaSuccess) return fail(ION_E_CUDA, "kernel launch: %s (%s:%d)", cudaGetErrorString(e_), \
+                                           __FILE__, __LINE__);                                       \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// Units -> kernel constants (src/lbm/units.rs:259-307; domain.rs:808, 839, 848),
+// evaluated in the same f32/f64 steps as the Rust code.
+// ---------------------------------------------------------------------------
+float sqf(float x) { return x * x; }
+float cbf(float x) { return x * x * x; }
+float to4f(float x) { return x * x * x * x; }
+double atom_mass(int p) {
+    switch (p) {
+        case ION_PROP_HE: return 6.6464731e-27;
+        case ION_PROP_NE: return 3.3509177e-26;
+        case ION_PROP_AR: return 6.6335209e-26;
+        case ION_PROP_KR: return 1.3914984e-25;
+        case ION_PROP_XE: return 2.1801714e-25;
+        default: return 1.6735575e-27;
+    }
+}
+void derive_constants(const ion_config& c, ion_constants& k) {
+    const ion_units& u = c.units;
+    const float pi = (float)3.14159265358979323846;
+    memset(&k, 0, sizeof k);
+    k.w = 1.0f / (3.0f * c.nu + 0.5f);
+    k.epsilon_0 = 8.8541878128E-12f / ((sqf(u.a) * to4f(u.s)) / (u.kg * cbf(u.m)));
+    k.ke = 1.0f / (4.0f * pi * k.epsilon_0);
+    k.mu_0 = 1.256637062E-6f / ((u.kg * u.m) / (sqf(u.a) * sqf(u.s)));
+    k.kmu = k.mu_0 / (4.0f * pi);
+    k.kmu0 = k.mu_0;
+    k.kkge = (float)(9.1093837139E-31 / -1.602176634E-19) / (u.kg / (u.a * u.s));
+    k.kimg = (float)((1.0 / (atom_mass(u.prop) * 1e20)) / (double)u.kg);
+    k.kvev = (float)(9.1093837139E-31 / (2.0 * 1.602176634E-19) / (double)u.kg);
+    k.kme = (float)(5.68563006E-12 / ((double)u.kg / ((double)u.a * (double)u.s)));
+    k.wq = 1.0f / (2.0f * 1.0f + 0.5f);
+}
+
+int velocity_q(int vs) { return vs == ION_D2Q9 ? 9 : vs == ION_D3Q15 ? 15 : vs == ION_D3Q19 ? 19 : 27; }
+
+int validate(const ion_config& c) {
+    if (c.d_x != 1 || c.d_y != 1 || c.d_z != 1)
+        return fail(ION_E_CONFIG, "d_x, d_y, d_z must be 1: this build runs one domain on one GPU");
+    if (c.velocity_set == ION_D3Q27)
+        return fail(ION_E_CONFIG, "D3Q27: the reference defines no DEF_WC for it (domain.rs:766-768), so it does not build");
+    if (c.velocity_set < ION_D2Q9 || c.velocity_set > ION_D3Q19) return fail(ION_E_CONFIG, "unknown velocity_set %d", c.velocity_set);
+    if (c.relaxation_time != ION_SRT && c.relaxation_time != ION_TRT) return fail(ION_E_CONFIG, "unknown relaxation_time");
+    if (c.float_type < ION_FP16S || c.float_type > ION_FP32) return fail(ION_E_CONFIG, "unknown float_type");
+    if (c.n_x == 0 || c.n_y == 0 || c.n_z == 0) return fail(ION_E_CONFIG, "grid sizes must be >= 1");
+    const uint64_t n = (uint64_t)c.n_x * c.n_y * c.n_z;
+    if (n >= (1ull << 32)) return fail(ION_E_CONFIG, "more than 2^32-1 cells (the reference indexes cells with uint)");
+    if (c.velocity_set == ION_D2Q9 && c.n_z != 1) return fail(ION_E_CONFIG, "D2Q9 needs n_z == 1");
+    if (c.ext_subgrid_ecr) return fail(ION_E_CONFIG, "the SUBGRID_ECR extension is not part of this build");
+    if (c.ext_magneto_hydro) {
+        if (!c.ext_volume_force) return fail(ION_E_CONFIG, "ext_magneto_hydro needs ext_volume_force (as in the reference)");
+        if (c.velocity_set == ION_D2Q9)
+            return fail(ION_E_CONFIG, "ext_magneto_hydro needs a 3D velocity set (the reference divides by n_z/2^D = 0)");
+        if (c.mhd_lod_depth > 4) return fail(ION_E_CONFIG, "mhd_lod_depth > 4 is not supported");
+        const uint32_t nd = 1u << c.mhd_lod_depth;
+        if (c.n_x % nd || c.n_y % nd || c.n_z % nd)
+            return fail(ION_E_CONFIG, "with ext_magneto_hydro, n_x/n_y/n_z must be multiples of 2^mhd_lod_depth");
+        if (c.field_mode != ION_FIELD_BITWISE && c.field_mode != ION_FIELD_FAST)
+            return fail(ION_E_CONFIG, "field_mode %d is not available", (int)c.field_mode);
+    }
+    if (c.ext_force_field && !c.ext_volume_force) return fail(ION_E_CONFIG, "ext_force_field needs ext_volume_force");
+    return ION_OK;
+}
+
+__global__ void k_fill(float* p, uint64_t n, float v) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
+struct HostMesh {
+    std::vector<float> p0, p1, p2;  // [ntri][3]
+    uint32_t ntri = 0;
+    float pmin[3] = {0, 0, 0}, pmax[3] = {0, 0, 0}, center[3] = {0, 0, 0};
+    // Mesh::update_bounds, src/mesh.rs:94-109
+    void update_bounds() {
+        if (!ntri) return;
+        for (int a = 0; a < 3; a++) pmin[a] = pmax[a] = p0[a];
+        for (uint32_t i = 0; i < ntri; i++)
+            for (int a = 0; a < 3; a++) {
+                const float x0 = p0[3 * i + a], x1 = p1[3 * i + a], x2 = p2[3 * i + a];
+                pmin[a] = std::fmin(pmin[a], std::fmin(x2, std::fmin(x1, x0)));
+                pmax[a] = std::fmax(pmax[a], std::fmax(x2, std::fmax(x1, x0)));
+            }
+    }
+};
+
+struct KEv {
+    int kernel;
+    cudaEvent_t a, b;
+};
+
+}  // namespace
+
+struct ion_lbm {
+    ion_config cfg{};
+    ion_constants k{};
+    DevLbm L{};
+    cudaStream_t stream = nullptr;
+    int q = 19;
+    uint64_t t = 0;
+    bool initialized = false;
+    size_t e_dyn_count = 0;
+    uint32_t* d_err = nullptr;
+    double* d_partials = nullptr;
+    double* d_sums = nullptr;
+    uint32_t nparts = 0;
+    uint32_t* d_tiles = nullptr;
+    uint32_t* d_list = nullptr;
+    uint32_t* d_count = nullptr;
+    float *d_p0 = nullptr, *d_p1 = nullptr, *d_p2 = nullptr;
+    size_t tri_cap = 0;
+    std::vector<HostMesh> meshes;
+    cudaGraphExec_t graph = nullptr;
+    uint32_t graph_kernels = 0;
+    cudaEvent_t ev[8] = {};
+    bool ktiming = false;
+    std::vector<KEv> kev;
+    std::vector<cudaEvent_t> ev_pool;
+    double ktime[3] = {0, 0, 0};
+    uint64_t kcount[3] = {0, 0, 0};
+    std::vector<void*> allocs;
+};
+
+namespace {
+
+int dmalloc(ion_lbm* h, void** p, size_t bytes) {
+    *p = nullptr;
+    if (!bytes) return ION_OK;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ION_E_NOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+    }
+    h->allocs.push_back(*p);
+    return cudaMemsetAsync(*p, 0, bytes, h->stream) == cudaSuccess ? ION_OK : fail(ION_E_CUDA, "cudaMemsetAsync");
+}
+
+size_t ddf_bytes(int ft) { return ft == ION_FP32 ? 4 : 2; }
+
+void destroy_handle(ion_lbm* h) {
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    for (void* p : h->allocs) cudaFree(p);
+    for (auto& e : h->ev) if (e) cudaEventDestroy(e);
+    for (auto& e : h->kev) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
+    for (auto e : h->ev_pool) cudaEventDestroy(e);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+// -------- launches of one step ---------------------------------------------
+int launch_stream_collide(ion_lbm* h, uint64_t t) {
+    const int ft = h->cfg.float_type;
+    const bool mhd = h->cfg.ext_magneto_hydro, trt = h->cfg.relaxation_time == ION_TRT;
+    if (h->q == 19) q19_stream_collide(h->L, ft, mhd, trt, t, h->stream);
+    else if (h->q == 15) q15_stream_collide(h->L, ft, mhd, trt, t, h->stream);
+    else q9_stream_collide(h->L, ft, mhd, trt, t, h->stream);
+    g_launches++;
+    CKL();
+    return ION_OK;
+}
+
+int launch_field(ion_lbm* h) {
+    launch_update_e_b(h->L, h->cfg.field_mode == ION_FIELD_FAST, h->d_err, h->stream);
+    g_launches++;
+    CKL();
+    return ION_OK;
+}
+
+int launch_bins(ion_lbm* h) {
+    if (h->L.depth > 0) {
+        launch_lod_bins(h->L, h->stream);
+        g_launches++;
+        CKL();
+    } else {
+        CK(cudaMemsetAsync(h->L.qu_lod, 0, sizeof(float) * 4 * (size_t)h->L.n_lod_own, h->stream));
+    }
+    return ION_OK;
+}
+
+cudaEvent_t pool_event(ion_lbm* h) {
+    if (!h->ev_pool.empty()) { cudaEvent_t e = h->ev_pool.back(); h->ev_pool.pop_back(); return e; }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+template <class F>
+int timed(ion_lbm* h, int kernel, F&& f) {
+    if (!h->ktiming) return f();
+    KEv r{kernel, pool_event(h), pool_event(h)};
+    cudaEventRecord(r.a, h->stream);
+    const int rc = f();
+    cudaEventRecord(r.b, h->stream);
+    h->kev.push_back(r);
+    return rc;
+}
+
+// Lbm::do_time_step (src/lbm/mod.rs:250-272) for step t
+int enqueue_step(ion_lbm* h, uint64_t t) {
+    int rc = timed(h, 0, [&] { return launch_stream_collide(h, t); });
+    if (rc) return rc;
+    if (h->cfg.ext_magneto_hydro) {
+        rc = timed(h, 2, [&] { return launch_bins(h); });
+        if (rc) return rc;
+        rc = timed(h, 1, [&] { return launch_field(h); });
+        if (rc) return rc;
+    }
+    return ION_OK;
+}
+
+uint32_t kernels_per_step(const ion_lbm* h) {
+    return 1u + (h->cfg.ext_magneto_hydro ? (h->L.depth > 0 ? 2u : 1u) : 0u);
+}
+
+int check_device_error(ion_lbm* h) {
+    uint32_t err = 0;
+    CK(cudaMemcpyAsync(&err, h->d_err, 4, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (err) {
+        CK(cudaMemsetAsync(h->d_err, 0, 4, h->stream));
+        return fail(ION_E_TIMEOUT, "a field-kernel shared-memory tile did not arrive within its wait limit");
+    }
+    return ION_OK;
+}
+
+// -------- STL (Mesh::read_stl_raw, src/mesh.rs:175-220) --------------------
+struct Mat3 { float xx, xy, xz, yx, yy, yz, zx, zy, zz; };
+Mat3 rot_around(float vx, float vy, float vz, float r) {  // src/mesh.rs:57-66
+    const float sr = std::sin(r), cr = std::cos(r);
+    auto sq = [](float x) { return x * x; };
+    Mat3 m;
+    m.xx = sq(vx) + (1.0f - sq(vx)) * cr; m.xy = vx * vy * (1.0f - cr) - vz * sr; m.xz = vx * vz * (1.0f - cr) + vy * sr;
+    m.yx = vx * vy * (1.0f - cr) + vz * sr; m.yy = sq(vy) + (1.0f - sq(vy)) * cr; m.yz = vy * vz * (1.0f - cr) - vx * sr;
+    m.zx = vx * vz * (1.0f - cr) - vy * sr; m.zy = vy * vz * (1.0f - cr) + vx * sr; m.zz = sq(vz) + (1.0f - sq(vz)) * cr;
+    return m;
+}
+Mat3 matmul(const Mat3& a, const Mat3& m) {  // src/mesh.rs:419-428
+    Mat3 r;
+    r.xx = a.xx * m.xx + a.xy * m.yx + a.xz * m.zx; r.xy = a.xx * m.xy + a.xy * m.yy + a.xz * m.zy; r.xz = a.xx * m.xz + a.xy * m.yz + a.xz * m.zz;
+    r.yx = a.yx * m.xx + a.yy * m.yx + a.yz * m.zx; r.yy = a.yx * m.xy + a.yy * m.yy + a.yz * m.zy; r.yz = a.yx * m.xz + a.yy * m.yz + a.yz * m.zz;
+    r.zx = a.zx * m.xx + a.zy * m.yx + a.zz * m.zx; r.zy = a.zx * m.xy + a.zy * m.yy + a.zz * m.zy; r.zz = a.zx * m.xz + a.zy * m.yz + a.zz * m.zz;
+    return r;
+}
+Mat3 rotation_deg(float rx, float ry, float rz) {  // construct_rotation_matrix, src/mesh.rs:51-55
+    const float pi = (float)3.14159265358979323846;
+    return matmul(matmul(rot_around(1, 0, 0, rx * pi / 180.0f), rot_around(0, 1, 0, ry * pi / 180.0f)),
+                  rot_around(0, 0, 1, rz * pi / 180.0f));
+}
+
+int read_stl(const char* path, bool reposition, const float box[3], const float center[3], const Mat3& R, float size,
+             HostMesh& mesh) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return fail(ION_E_IO, "could not open or find file \"%s\"", path);
+    std::vector<unsigned char> buf((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    if (buf.size() < 84) return fail(ION_E_FORMAT, "\"%s\" is corrupted or unsupported (only binary .stl)", path);
+    auto u32 = [&](size_t o) { return (uint32_t)buf[o] | ((uint32_t)buf[o + 1] << 8) | ((uint32_t)buf[o + 2] << 16) | ((uint32_t)buf[o + 3] << 24); };
+    auto f32 = [&](size_t o) { const uint32_t u = u32(o); float v; memcpy(&v, &u, 4); return v; };
+    const uint32_t nt = u32(80);
+    if (nt == 0 || buf.size() != 84ull + 50ull * nt)
+        return fail(ION_E_FORMAT, "\"%s\" is corrupted or unsupported (only binary .stl)", path);
+    mesh = HostMesh();
+    mesh.ntri = nt;
+    mesh.p0.resize(3 * (size_t)nt); mesh.p1.resize(3 * (size_t)nt); mesh.p2.resize(3 * (size_t)nt);
+    for (int a = 0; a < 3; a++) mesh.center[a] = center[a];
+    size_t o = 84;
+    for (uint32_t i = 0; i < nt; i++) {
+        o += 12;  // normal
+        float* dst[3] = {&mesh.p0[3 * (size_t)i], &mesh.p1[3 * (size_t)i], &mesh.p2[3 * (size_t)i]};
+        for (int v = 0; v < 3; v++) {
+            const float x = f32(o), y = f32(o + 4), z = f32(o + 8);
+            o += 12;
+            dst[v][0] = R.xx * x + R.xy * y + R.xz * z;
+            dst[v][1] = R.yx * x + R.yy * y + R.yz * z;
+            dst[v][2] = R.zx * x + R.zy * y + R.zz * z;
+        }
+        o += 2;  // attribute bits
+    }
+    mesh.update_bounds();
+    float scale;
+    if (size == 0.0f) {
+        scale = std::fmin(box[0] / (mesh.pmax[0] - mesh.pmin[0]),
+                          std::fmin(box[1] / (mesh.pmax[1] - mesh.pmin[1]), box[2] / (mesh.pmax[2] - mesh.pmin[2])));
+    } else if (size > 0.0f) {
+        const float mx = std::fmax(mesh.pmax[0] - mesh.pmin[0], std::fmax(mesh.pmax[1] - mesh.pmin[1], mesh.pmax[2] - mesh.pmin[2]));
+        scale = size / mx;
+    } else {
+        scale = -size;
+    }
+    float off[3] = {0, 0, 0};
+    if (reposition) for (int a = 0; a < 3; a++) off[a] = -0.5f * (mesh.pmin[a] + mesh.pmax[a]);
+    for (std::vector<float>* p : {&mesh.p0, &mesh.p1, &mesh.p2})
+        for (uint32_t i = 0; i < nt; i++)
+            for (int a = 0; a < 3; a++) (*p)[3 * (size_t)i + a] = center[a] + scale * (off[a] + (*p)[3 * (size_t)i + a]);
+    mesh.update_bounds();
+    return ION_OK;
+}
+
+// -------- .ion byte stream (src/file.rs:336-433) ---------------------------
+struct Reader {
+    const std::vector<unsigned char>& b;
+    size_t pos = 0;
+    bool ok = true;
+    bool need(size_t n) { if (pos + n > b.size()) ok = false; return ok; }
+    uint8_t u8() { if (!need(1)) return 0; return b[pos++]; }
+    uint32_t u32() { if (!need(4)) return 0; uint32_t v = 0; for (int i = 0; i < 4; i++) v |= (uint32_t)b[pos++] << (8 * i); return v; }
+    uint64_t u64() { if (!need(8)) return 0; uint64_t v = 0; for (int i = 0; i < 8; i++) v |= (uint64_t)b[pos++] << (8 * i); return v; }
+    float f32() { const uint32_t u = u32(); float f; memcpy(&f, &u, 4); return f; }
+};
+void push32(std::vector<unsigned char>& v, uint32_t x) { for (int i = 0; i < 4; i++) v.push_back((unsigned char)(x >> (8 * i))); }
+void pushf(std::vector<unsigned char>& v, float f) { uint32_t u; memcpy(&u, &f, 4); push32(v, u); }
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int ion_abi_version(void) { return ION_ABI_VERSION; }
+const char* ion_last_error(void) { return g_error.c_str(); }
+uint64_t ion_kernel_launch_count(void) { return g_launches.load(); }
+
+int ion_units_default(ion_units* u) {
+    if (!u) return fail(ION_E_INVALID, "null units");
+    u->m = 1.0f; u->kg = 1.0f; u->s = 1.0f; u->a = 1.0f; u->k = 1.0f; u->prop = ION_PROP_H;
+    return ION_OK;
+}
+
+int ion_units_set(ion_units* u, float lbm_length, float lbm_velocity, float lbm_rho, float lbm_charge, float lbm_temp,
+                  float si_length, float si_velocity, float si_rho, float si_charge, float si_temp) {
+    if (!u) return fail(ION_E_INVALID, "null units");
+    u->m = si_length / lbm_length;                  // src/lbm/units.rs:164-168
+    u->kg = si_rho / lbm_rho * cbf(u->m);
+    u->s = u->m / (si_velocity / lbm_velocity);
+    u->a = si_charge / lbm_charge / u->s;
+    u->k = si_temp / lbm_temp;
+    return ION_OK;
+}
+
+int ion_units_si_to_lu(const ion_units* u, int what, float v, float* out) {
+    if (!u || !out) return fail(ION_E_INVALID, "null argument");
+    switch (what) {
+        case 0: *out = v / (sqf(u->m) / u->s); break;  // nu_si_lu
+        case 1: *out = v / (u->a / u->m); break;       // magnetization_si_lu
+        case 2: *out = v / (u->a * u->s); break;       // charge_si_lu
+        case 3: *out = v / u->m; break;                // len_si_lu
+        default: return fail(ION_E_INVALID, "unknown conversion %d", what);
+    }
+    return ION_OK;
+}
+
+int ion_config_default(ion_config* c) {
+    if (!c) return fail(ION_E_INVALID, "null config");
+    memset(c, 0, sizeof *c);
+    c->velocity_set = ION_D2Q9;
+    c->relaxation_time = ION_SRT;
+    c->float_type = ION_FP16S;
+    ion_units_default(&c->units);
+    c->n_x = c->n_y = c->n_z = 1;
+    c->d_x = c->d_y = c->d_z = 1;
+    c->nu = 1.0f / 6.0f;
+    c->mhd_lod_depth = 4;
+    c->update_fields = 1;  // graphics_active defaults to true (graphics.rs:160)
+    c->field_mode = ION_FIELD_BITWISE;
+    return ION_OK;
+}
+
+int ion_constants_from_config(const ion_config* c, ion_constants* k) {
+    if (!c || !k) return fail(ION_E_INVALID, "null argument");
+    derive_constants(*c, *k);
+    return ION_OK;
+}
+
+int ion_lbm_create(const ion_config* cfg, ion_lbm** out) {
+    if (!cfg || !out) return fail(ION_E_INVALID, "null argument");
+    *out = nullptr;
+    int rc = validate(*cfg);
+    if (rc) return rc;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaFree(0) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ION_E_CUDA, "no usable CUDA device");
+    }
+    ion_lbm* h = new ion_lbm();
+    h->cfg = *cfg;
+    derive_constants(*cfg, h->k);
+    h->q = velocity_q(cfg->velocity_set);
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete h;
+        return fail(ION_E_CUDA, "cudaStreamCreate failed");
+    }
+    DevLbm& L = h->L;
+    L.nx = cfg->n_x; L.ny = cfg->n_y; L.nz = cfg->n_z;
+    L.n = cfg->n_x * cfg->n_y * cfg->n_z;
+    L.dx = FastDiv(L.nx);
+    L.dxy = FastDiv(L.nx * L.ny);
+    const size_t N = L.n, db = ddf_bytes(cfg->float_type);
+    const bool mhd = cfg->ext_magneto_hydro;
+    auto A = [&](void** p, size_t bytes) { return rc ? rc : (rc = dmalloc(h, p, bytes)); };
+    A(&L.fi, N * h->q * db);
+    A((void**)&L.rho, N * 4);
+    A((void**)&L.u, 3 * N * 4);
+    A((void**)&L.flags, N);
+    if (cfg->ext_force_field) A((void**)&L.F, 3 * N * 4);
+    uint32_t depth = cfg->mhd_lod_depth, nd = 1u << depth;
+    uint32_t n_lod_own = 1;
+    for (uint32_t i = 0; i < depth; i++) n_lod_own += (1u << (i + 1)) * (1u << (i + 1)) * (1u << (i + 1));
+    if (mhd) {
+        const size_t npsi = (size_t)(L.nx + 2) * (L.ny + 2) * (L.nz + 2);
+        h->e_dyn_count = npsi > 3 * N ? npsi : 3 * N;
+        A((void**)&L.e_stat, 3 * N * 4);
+        A((void**)&L.b_stat, 3 * N * 4);
+        A((void**)&L.e_dyn, h->e_dyn_count * 4);
+        A((void**)&L.b_dyn, 3 * N * 4);
+        A(&L.fqi, 7 * N * db);
+        A(&L.ei, N * h->q * db);
+        A((void**)&L.q, N * 4);
+        A((void**)&L.qu_lod, (size_t)n_lod_own * 16);
+        if (depth > 0) A((void**)&L.lod_cell, 3 * N * 4);
+        A((void**)&L.lod_pos, (size_t)n_lod_own * 16);
+    }
+    A((void**)&h->d_err, 4);
+    h->nparts = 1024;
+    A((void**)&h->d_partials, h->nparts * sizeof(double));
+    A((void**)&h->d_sums, 4 * sizeof(double));
+    A((void**)&h->d_count, 2 * sizeof(uint32_t));
+    if (rc) { destroy_handle(h); return rc; }
+    k_fill<<<grid_for(N, 256), 256, 0, h->stream>>>(L.rho, N, 1.0f);  // rho starts at 1 (domain.rs:156)
+    g_launches++;
+    L.w = h->k.w; L.ke = h->k.ke; L.kmu = h->k.kmu; L.kmu0 = h->k.kmu0; L.kkge = h->k.kkge; L.wq = h->k.wq;
+    L.fx = cfg->f_x; L.fy = cfg->f_y; L.fz = cfg->f_z;
+    L.ext_eq = cfg->ext_equilibrium_boundaries; L.ext_vf = cfg->ext_volume_force; L.ext_ff = cfg->ext_force_field;
+    L.ext_mhd = mhd; L.update_fields = cfg->update_fields;
+    L.depth = depth; L.nd = nd; L.n_lod_own = n_lod_own;
+    L.n_bins = nd * nd * nd;
+    L.first_src = n_lod_own > L.n_bins ? n_lod_own - L.n_bins : 0u;
+    if (mhd) {
+        L.bsx = L.nx / nd; L.bsy = L.ny / nd; L.bsz = L.nz / nd;
+        L.ils = 1.0f / (float)(L.bsx * L.bsy * L.bsz);  // 1/lod_s(D), sim_kernels.cl:435-438, 672
+        const uint32_t big = 1u << nd;                   // near block NX/(1<<(1<<D)), sim_kernels.cl:907-910
+        L.near_x = std::max(L.nx / big, 1u); L.near_y = std::max(L.ny / big, 1u); L.near_z = std::max(L.nz / big, 1u);
+        // LOD bin centres, lod_coordinates (sim_kernels.cl:440-447)
+        std::vector<float4> pos(n_lod_own);
+        const float dsx = (float)(L.nx / nd), dsy = (float)(L.ny / nd), dsz = (float)(L.nz / nd);
+        for (uint32_t d = 0; d < n_lod_own; d++) {
+            const uint32_t tt = d % (nd * nd);
+            pos[d] = make_float4((float)(tt % nd) * dsx + (0.5f * dsx), (float)(tt / nd) * dsy + (0.5f * dsy),
+                                 (float)(d / (nd * nd)) * dsz + (0.5f * dsz), 0.0f);
+        }
+        if (cudaMemcpyAsync(L.lod_pos, pos.data(), pos.size() * 16, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+            cudaStreamSynchronize(h->stream) != cudaSuccess) {
+            destroy_handle(h);
+            return fail(ION_E_CUDA, "upload of LOD centres failed");
+        }
+    }
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) { destroy_handle(h); return fail(ION_E_CUDA, "create: stream sync failed"); }
+    for (auto& e : h->ev) cudaEventCreate(&e);
+    *out = h;
+    return ION_OK;
+}
+
+int ion_lbm_destroy(ion_lbm* h) {
+    destroy_handle(h);
+    return ION_OK;
+}
+
+int ion_lbm_get_config(const ion_lbm* h, ion_config* out) {
+    if (!h || !out) return fail(ION_E_INVALID, "null argument");
+    *out = h->cfg;
+    return ION_OK;
+}
+
+int ion_lbm_initialize(ion_lbm* h) {
+    if (!h) return fail(ION_E_INVALID, "null handle");
+    const int ft = h->cfg.float_type;
+    const bool mhd = h->cfg.ext_magneto_hydro;
+    h->t = 1;
+    if (h->q == 19) q19_initialize(h->L, ft, mhd, h->stream);
+    else if (h->q == 15) q15_initialize(h->L, ft, mhd, h->stream);
+    else q9_initialize(h->L, ft, mhd, h->stream);
+    g_launches++;
+    CKL();
+    if (mhd) {
+        int rc = launch_field(h);
+        if (rc) return rc;
+    }
+    h->t = 0;
+    h->initialized = true;
+    return ION_OK;
+}
+
+int ion_lbm_do_time_step(ion_lbm* h) {
+    if (!h) return fail(ION_E_INVALID, "null handle");
+    int rc = enqueue_step(h, h->t);
+    if (rc) return rc;
+    h->t += 1;
+    return ION_OK;
+}
+
+int ion_lbm_run(ion_lbm* h, uint64_t steps) {
+    if (!h) return fail(ION_E_INVALID, "null handle");
+    if (!h->initialized) {
+        int rc = ion_lbm_initialize(h);
+        if (rc) return rc;
+    }
+    if (h->ktiming || steps < 4) {
+        for (uint64_t i = 0; i < steps; i++) {
+            int rc = ion_lbm_do_time_step(h);
+            if (rc) return rc;
+        }
+        return ION_OK;
+    }
+    if (h->t & 1u) {  // the graph holds an even step followed by an odd one
+        int rc = ion_lbm_do_time_step(h);
+        if (rc) return rc;
+        steps--;
+    }
+    if (!h->graph) {
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue_step(h, 0);
+        if (!rc) rc = enqueue_step(h, 1);
+        cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+        if (rc) return rc;
+        if (e != cudaSuccess) return fail(ION_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&h->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { h->graph = nullptr; return fail(ION_E_CUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
+        h->graph_kernels = 2 * kernels_per_step(h);
+        g_launches -= h->graph_kernels;  // capture does not launch
+    }
+    for (uint64_t i = 0; i + 1 < steps; i += 2) {
+        CK(cudaGraphLaunch(h->graph, h->stream));
+        g_launches += h->graph_kernels;
+        h->t += 2;
+    }
+    if (steps & 1u) return ion_lbm_do_time_step(h);
+    return ION_OK;
+}
+
+int ion_lbm_get_time_step(const ion_lbm* h, uint64_t* t) {
+    if (!h || !t) return fail(ION_E_INVALID, "null argument");
+    *t = h->t;
+    return ION_OK;
+}
+
+int ion_lbm_finish_queues(ion_lbm* h, int timeout_ms) {
+    if (!h) return fail(ION_E_INVALID, "null handle");
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        const cudaError_t e = cudaStreamQuery(h->stream);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady) return fail(ION_E_CUDA, "stream: %s", cudaGetErrorString(e));
+        if (timeout_ms >= 0 && std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(timeout_ms))
+            return fail(ION_E_TIMEOUT, "stream still busy after %d ms", timeout_ms);
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    return h->cfg.ext_magneto_hydro ? check_device_error(h) : ION_OK;
+}
+
+int ion_lbm_update_fields(ion_lbm* h) {
+    if (!h) return fail(ION_E_INVALID, "null handle");
+    const int ft = h->cfg.float_type;
+    if (h->q == 19) q19_update_fields(h->L, ft, h->t, h->stream);
+    else if (h->q == 15) q15_update_fields(h->L, ft, h->t, h->stream);
+    else q9_update_fields(h->L, ft, h->t, h->stream);
+    g_launches++;
+    CKL();
+    return ION_OK;
+}
+
+static void* field_ptr(ion_lbm* h, int f, size_t* eb, size_t* count) {
+    const size_t N = h->L.n, db = ddf_bytes(h->cfg.float_type);
+    const bool mhd = h->cfg.ext_magneto_hydro;
+    void* p = nullptr;
+    size_t e = 4, c = 0;
+    switch (f) {
+        case ION_FIELD_FI: p = h->L.fi; e = db; c = N * h->q; break;
+        case ION_FIELD_RHO: p = h->L.rho; c = N; break;
+        case ION_FIELD_U: p = h->L.u; c = 3 * N; break;
+        case ION_FIELD_FLAGS: p = h->L.flags; e = 1; c = N; break;
+        case ION_FIELD_F: p = h->L.F; c = h->L.F ? 3 * N : 0; break;
+        case ION_FIELD_E_STAT: p = h->L.e_stat; c = mhd ? 3 * N : 0; break;
+        case ION_FIELD_B_STAT: p = h->L.b_stat; c = mhd ? 3 * N : 0; break;
+        case ION_FIELD_E_DYN: p = h->L.e_dyn; c = mhd ? h->e_dyn_count : 0; break;
+        case ION_FIELD_B_DYN: p = h->L.b_dyn; c = mhd ? 3 * N : 0; break;
+        case ION_FIELD_FQI: p = h->L.fqi; e = db; c = mhd ? 7 * N : 0; break;
+        case ION_FIELD_EI: p = h->L.ei; e = db; c = mhd ? N * h->q : 0; break;
+        case ION_FIELD_Q: p = h->L.q; c = mhd ? N : 0; break;
+        case ION_FIELD_QU_LOD: p = h->L.qu_lod; c = mhd ? 4 * (size_t)h->L.n_lod_own : 0; break;
+        default: break;
+    }
+    if (eb) *eb = e;
+    if (count) *count = c;
+    return c ? p : nullptr;
+}
+
+int ion_lbm_field_info(const ion_lbm* h, int field, size_t* elem_bytes, size_t* count) {
+    if (!h) return fail(ION_E_INVALID, "null handle");
+    if (field < 0 || field >= ION_FIELD_COUNT) return fail(ION_E_INVALID, "unknown field %d", field);
+    field_ptr(const_cast<ion_lbm*>(h), field, elem_bytes, count);
+    return ION_OK;
+}
+
+int ion_lbm_write_field(ion_lbm* h, int field, const void* host, size_t bytes) {
+    if (!h || !host) return fail(ION_E_INVALID, "null argument");
+    size_t eb, c;
+    void* p = field_ptr(h, field, &eb, &c);
+    if (!p) return fail(ION_E_INVALID, "field %d is not present in this configuration", field);
+    if (bytes > eb * c) return fail(ION_E_INVALID, "field %d holds %zu bytes, got %zu", field, eb * c, bytes);
+    CK(cudaMemcpyAsync(p, host, bytes, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return ION_OK;
+}
+
+int ion_lbm_read_field(ion_lbm* h, int field, void* host, size_t bytes) {
+    if (!h || !host) return fail(ION_E_INVALID, "null argument");
+    size_t eb, c;
+    void* p = field_ptr(h, field, &eb, &c);
+    if (!p) return fail(ION_E_INVALID, "field %d is not present in this configuration", field);
+    if (bytes > eb * c) return fail(ION_E_INVALID, "field %d holds %zu bytes, asked for %zu", field, eb * c, bytes);
+    CK(cudaMemcpyAsync(host, p, bytes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return h->cfg.ext_magneto_hydro ? check_device_error(h) : ION_OK;
+}
+
+int ion_lbm_field_device_ptr(ion_lbm* h, int field, void** dptr, size_t* bytes) {
+    if (!h || !dptr) return fail(ION_E_INVALID, "null argument");
+    size_t eb, c;
+    *dptr = field_ptr(h, field, &eb, &c);
+    if (bytes) *bytes = eb * c;
+    return *dptr ? ION_OK : fail(ION_E_INVALID, "field %d is not present", field);
+}
+
+int ion_lbm_stream(ion_lbm* h, void** s) {
+    if (!h || !s) return fail(ION_E_INVALID, "null argument");
+    *s = (void*)h->stream;
+    return ION_OK;
+}
+
+// ---- meshes ----------------------------------------------------------------
+int ion_lbm_add_mesh(ion_lbm* h, const float* p0, const float* p1, const float* p2, uint32_t ntri, uint32_t* index) {
+    if (!h || !p0 || !p1 || !p2 || ntri == 0) return fail(ION_E_INVALID, "empty or null mesh");
+    HostMesh m;
+    m.ntri = ntri;
+    m.p0.assign(p0, p0 + 3 * (size_t)ntri);
+    m.p1.assign(p1, p1 + 3 * (size_t)ntri);
+    m.p2.assign(p2, p2 + 3 * (size_t)ntri);
+    m.update_bounds();
+    for (int a = 0; a < 3; a++) m.center[a] = 0.5f * (m.pmin[a] + m.pmax[a]);
+    h->meshes.push_back(std::move(m));
+    if (index) *index = (uint32_t)h->meshes.size() - 1;
+    return ION_OK;
+}
+
+int ion_lbm_import_mesh(ion_lbm* h, const char* path, float scale, float ox, float oy, float oz, float rx, float ry,
+                        float rz, uint32_t* index) {
+    if (!h || !path) return fail(ION_E_INVALID, "null argument");
+    const float box[3] = {1.0f, 1.0f, 1.0f}, c[3] = {ox, oy, oz};
+    const float scale_lu = scale / h->cfg.units.m;  // len_si_lu
+    HostMesh m;
+    int rc = read_stl(path, false, box, c, rotation_deg(rx, ry, rz), -std::fabs(scale_lu), m);
+    if (rc) return rc;
+    h->meshes.push_back(std::move(m));
+    if (index) *index = (uint32_t)h->meshes.size() - 1;
+    return ION_OK;
+}
+
+int ion_lbm_import_mesh_reposition(ion_lbm* h, const char* path, float cx, float cy, float cz, float rx, float ry,
+                                   float rz, float size, uint32_t* index) {
+    if (!h || !path) return fail(ION_E_INVALID, "null argument");
+    const float box[3] = {(float)h->cfg.n_x, (float)h->cfg.n_y, (float)h->cfg.n_z}, c[3] = {cx, cy, cz};
+    HostMesh m;
+    int rc = read_stl(path, true, box, c, rotation_deg(rx, ry, rz), size, m);
+    if (rc) return rc;
+    h->meshes.push_back(std::move(m));
+    if (index) *index = (uint32_t)h->meshes.size() - 1;
+    return ION_OK;
+}
+
+int ion_lbm_mesh_translate(ion_lbm* h, uint32_t index, float dx, float dy, float dz) {
+    if (!h || index >= h->meshes.size()) return fail(ION_E_INVALID, "no mesh %u", index);
+    HostMesh& m = h->meshes[index];
+    const float d[3] = {dx, dy, dz};
+    for (std::vector<float>* p : {&m.p0, &m.p1, &m.p2})
+        for (uint32_t i = 0; i < m.ntri; i++)
+            for (int a = 0; a < 3; a++) (*p)[3 * (size_t)i + a] += d[a];
+    for (int a = 0; a < 3; a++) { m.center[a] += d[a]; m.pmin[a] += d[a]; m.pmax[a] += d[a]; }
+    return ION_OK;
+}
+
+int ion_lbm_mesh_bounds(const ion_lbm* h, uint32_t index, float* out9) {
+    if (!h || !out9 || index >= h->meshes.size()) return fail(ION_E_INVALID, "no mesh %u", index);
+    const HostMesh& m = h->meshes[index];
+    for (int a = 0; a < 3; a++) { out9[a] = m.pmin[a]; out9[3 + a] = m.pmax[a]; out9[6 + a] = m.center[a]; }
+    return ION_OK;
+}
+
+// Lbm::voxelise_mesh -> LbmDomain::voxelize_mesh_on_device (src/mesh.rs:256-343)
+int ion_lbm_voxelise_mesh(ion_lbm* h, uint32_t index, int model_type, float v0, float v1, float v2) {
+    if (!h || index >= h->meshes.size()) return fail(ION_E_INVALID, "no mesh %u", index);
+    const HostMesh& m = h->meshes[index];
+    const size_t need = 3 * (size_t)m.ntri;
+    if (need > h->tri_cap) {
+        void* p;
+        int rc = 0;
+        if ((rc = dmalloc(h, &p, need * 4))) return rc;
+        h->d_p0 = (float*)p;
+        if ((rc = dmalloc(h, &p, need * 4))) return rc;
+        h->d_p1 = (float*)p;
+        if ((rc = dmalloc(h, &p, need * 4))) return rc;
+        h->d_p2 = (float*)p;
+        h->tri_cap = need;
+    }
+    CK(cudaMemcpyAsync(h->d_p0, m.p0.data(), need * 4, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_p1, m.p1.data(), need * 4, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_p2, m.p2.data(), need * 4, cudaMemcpyHostToDevice, h->stream));
+    VoxArgs A{};
+    A.p0 = h->d_p0; A.p1 = h->d_p1; A.p2 = h->d_p2; A.ntri = m.ntri;
+    A.x0 = m.pmin[0] - 2.0f; A.y0 = m.pmin[1] - 2.0f; A.z0 = m.pmin[2] - 2.0f;
+    A.x1 = m.pmax[0] + 2.0f; A.y1 = m.pmax[1] + 2.0f; A.z1 = m.pmax[2] + 2.0f;
+    const float c0 = (A.y1 - A.y0) * (A.z1 - A.z0), c1 = (A.z1 - A.z0) * (A.x1 - A.x0), c2 = (A.x1 - A.x0) * (A.y1 - A.y0);
+    A.direction = (c0 < c1 && c0 < c2) ? 0 : (c1 < c2 ? 1 : 2);
+    const uint32_t area[3] = {h->L.ny * h->L.nz, h->L.nx * h->L.nz, h->L.nx * h->L.ny};
+    A.columns = area[A.direction];
+    const ion_units& u = h->cfg.units;
+    switch (model_type) {
+        case ION_MODEL_SOLID: A.flag = 0x01; break;
+        case ION_MODEL_MAGNET: A.flag = 0x11; A.mx = v0 / (u.a / u.m); A.my = v1 / (u.a / u.m); A.mz = v2 / (u.a / u.m); break;
+        case ION_MODEL_CHARGED: A.flag = 0x09; A.mx = v0 / (u.a * u.s); break;
+        case ION_MODEL_CHARGED_ECR: A.flag = 0x05; A.mx = v0 / (u.a * u.s); break;
+        default: return fail(ION_E_INVALID, "unknown model type %d", model_type);
+    }
+    launch_voxelize(h->L, A, h->stream);
+    g_launches++;
+    CKL();
+    CK(cudaStreamSynchronize(h->stream));  // the host triangle arrays may change after return
+    return ION_OK;
+}
+
+static int ensure_compaction(ion_lbm* h) {
+    if (h->d_list) return ION_OK;
+    void* p;
+    int rc = dmalloc(h, &p, sizeof(uint32_t) * (((size_t)h->L.n + 1023) / 1024 + 1));
+    if (rc) return rc;
+    h->d_tiles = (uint32_t*)p;
+    rc = dmalloc(h, &p, sizeof(uint32_t) * (size_t)h->L.n);
+    if (rc) return rc;
+    h->d_list = (uint32_t*)p;
+    return ION_OK;
+}
+
+int ion_lbm_precompute_b(ion_lbm* h) {
+    if (!h) return fail(ION_E_INVALID, "null handle");
+    if (!h->cfg.ext_magneto_hydro) return fail(ION_E_STATE, "precompute_b needs ext_magneto_hydro");
+    int rc = ensure_compaction(h);
+    if (rc) return rc;
+    launch_compact(h->L, F_M, h->d_tiles, h->d_list, h->d_count, h->stream);
+    g_launches += 3;
+    launch_psi_static_b(h->L, h->d_list, h->d_count, h->stream);
+    g_launches += 2;
+    CKL();
+    CK(cudaStreamSynchronize(h->stream));
+    return ION_OK;
+}
+
+int ion_lbm_precompute_e(ion_lbm* h) {
+    if (!h) return fail(ION_E_INVALID, "null handle");
+    if (!h->cfg.ext_magneto_hydro) return fail(ION_E_STATE, "precompute_e needs ext_magneto_hydro");
+    int rc = ensure_compaction(h);
+    if (rc) return rc;
+    launch_compact(h->L, F_F | F_C, h->d_tiles, h->d_list, h->d_count, h->stream);
+    g_launches += 3;
+    launch_static_e(h->L, h->d_list, h->d_count, h->stream);
+    g_launches++;
+    CKL();
+    CK(cudaStreamSynchronize(h->stream));
+    return ION_OK;
+}
+
+int ion_lbm_mass_charge(ion_lbm* h, double* mass, double* charge) {
+    if (!h) return fail(ION_E_INVALID, "null handle");
+    const size_t N = h->L.n;
+    const int ft = h->cfg.float_type;
+    launch_sum_f64(h->L.fi, ft, N * h->q, h->d_partials, h->nparts, h->d_sums + 0, h->stream);
+    g_launches += 2;
+    if (h->cfg.ext_magneto_hydro) {
+        launch_sum_f64(h->L.fqi, ft, N * 7, h->d_partials, h->nparts, h->d_sums + 1, h->stream);
+        launch_sum_f64(h->L.ei, ft, N * h->q, h->d_partials, h->nparts, h->d_sums + 2, h->stream);
+        g_launches += 4;
+    }
+    CKL();
+    double s[3] = {0, 0, 0};
+    CK(cudaMemcpyAsync(s, h->d_sums, sizeof s, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    // DDFs are stored shifted by -w_i (sum_i w_i = 1 per cell): add N back
+    if (mass) *mass = s[0] + (double)N;
+    if (charge) *charge = h->cfg.ext_magneto_hydro ? (s[1] + (double)N) - (s[2] + (double)N) : 0.0;
+    return ION_OK;
+}
+
+// ---- .ion files (src/file.rs:42-306, FILE_LAYOUT.txt) -----------------------
+int ion_lbm_save(ion_lbm* h, const char* path) {
+    if (!h || !path) return fail(ION_E_INVALID, "null argument");
+    const ion_config& c = h->cfg;
+    const size_t N = h->L.n;
+    std::vector<unsigned char> b;
+    const char* hdr = "IonSolver setup\n";
+    b.insert(b.end(), hdr, hdr + 16);
+    b.push_back((unsigned char)c.velocity_set);
+    b.push_back((unsigned char)c.relaxation_time);
+    b.push_back((unsigned char)c.float_type);
+    pushf(b, c.units.m); pushf(b, c.units.kg); pushf(b, c.units.s); pushf(b, c.units.a);
+    push32(b, c.n_x); push32(b, c.n_y); push32(b, c.n_z);
+    b.push_back(0);  // fixed domains
+    push32(b, c.d_x); push32(b, c.d_y); push32(b, c.d_z);
+    pushf(b, c.nu); pushf(b, c.f_x); pushf(b, c.f_y); pushf(b, c.f_z);
+    b.push_back((unsigned char)((c.ext_equilibrium_boundaries ? 1 : 0) | (c.ext_volume_force ? 2 : 0) |
+                                (c.ext_force_field ? 4 : 0) | (c.ext_magneto_hydro ? 8 : 0)));
+    b.push_back(c.mhd_lod_depth);
+    const size_t head = b.size();
+    b.resize(head + N + 16 * N + (c.ext_magneto_hydro ? 4 * N : 0));
+    int rc = ion_lbm_read_field(h, ION_FIELD_FLAGS, b.data() + head, N);
+    if (!rc) rc = ion_lbm_read_field(h, ION_FIELD_RHO, b.data() + head + N, 4 * N);
+    if (!rc) rc = ion_lbm_read_field(h, ION_FIELD_U, b.data() + head + 5 * N, 12 * N);
+    if (!rc && c.ext_magneto_hydro) rc = ion_lbm_read_field(h, ION_FIELD_Q, b.data() + head + 17 * N, 4 * N);
+    if (rc) return rc;
+    // floats are little-endian on both supported hosts (x86-64, aarch64)
+    std::ofstream f(path, std::ios::binary);
+    if (!f) return fail(ION_E_IO, "writing went wrong: cannot open \"%s\"", path);
+    f.write((const char*)b.data(), (std::streamsize)b.size());
+    if (!f) return fail(ION_E_IO, "writing went wrong: \"%s\"", path);
+    return ION_OK;
+}
+
+int ion_lbm_load(const char* path, ion_config* cfg, ion_lbm** out) {
+    if (!path || !cfg || !out) return fail(ION_E_INVALID, "null argument");
+    *out = nullptr;
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return fail(ION_E_IO, "Could not find file.");
+    std::vector<unsigned char> buf((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    Reader r{buf};
+    char hdr[17] = {0};
+    for (int i = 0; i < 16; i++) hdr[i] = (char)r.u8();
+    if (!r.ok || strcmp(hdr, "IonSolver setup\n") != 0) return fail(ION_E_FORMAT, "Invalid Format!");
+    ion_config c = *cfg;
+    c.velocity_set = r.u8();
+    c.relaxation_time = r.u8();
+    c.float_type = r.u8();  // FloatType discriminants of types.rs:75-83 (the encoder's mapping)
+    c.units.m = r.f32(); c.units.kg = r.f32(); c.units.s = r.f32(); c.units.a = r.f32();
+    c.n_x = r.u32(); c.n_y = r.u32(); c.n_z = r.u32();
+    r.u8();  // fixed domains: skipped, as in the reference
+    c.d_x = r.u32(); c.d_y = r.u32(); c.d_z = r.u32();
+    c.nu = r.f32(); c.f_x = r.f32(); c.f_y = r.f32(); c.f_z = r.f32();
+    const uint8_t ext = r.u8();
+    c.ext_equilibrium_boundaries = (ext & 1) != 0;
+    c.ext_volume_force = (ext & 2) != 0;
+    c.ext_force_field = (ext & 4) != 0;
+    c.ext_magneto_hydro = (ext & 8) != 0;
+    c.mhd_lod_depth = r.u8();
+    if (!r.ok) return fail(ION_E_FORMAT, "file truncated in the config block");
+    const uint64_t N = (uint64_t)c.n_x * c.n_y * c.n_z;
+    const uint64_t body = N * 17 + (c.ext_magneto_hydro ? 4 * N : 0);
+    if (buf.size() - r.pos < body) return fail(ION_E_FORMAT, "Not all data could be read, file may be corrupted.");
+    const size_t o = r.pos;
+    r.pos += body;
+    if (c.ext_magneto_hydro && r.pos != buf.size()) {
+        // fixed charges and magnets (FILE_LAYOUT.txt:46-58): read and discarded,
+        // as the reference does; the reference's writer omits both sections.
+        const uint32_t nc = r.u32();
+        if (r.ok) r.pos += 12ull * nc;
+        const uint32_t nm = r.ok && r.pos <= buf.size() ? r.u32() : 0;
+        if (r.ok) r.pos += 20ull * nm;
+        if (!r.ok || r.pos > buf.size()) return fail(ION_E_FORMAT, "Not all data could be read, file may be corrupted.");
+    }
+    if (r.pos != buf.size()) return fail(ION_E_FORMAT, "Not all data could be read, file may be corrupted.");
+    ion_lbm* h = nullptr;
+    int rc = ion_lbm_create(&c, &h);
+    if (rc) return rc;
+    rc = ion_lbm_write_field(h, ION_FIELD_FLAGS, buf.data() + o, N);
+    if (!rc) rc = ion_lbm_write_field(h, ION_FIELD_RHO, buf.data() + o + N, 4 * N);
+    if (!rc) rc = ion_lbm_write_field(h, ION_FIELD_U, buf.data() + o + 5 * N, 12 * N);
+    if (!rc && c.ext_magneto_hydro) rc = ion_lbm_write_field(h, ION_FIELD_Q, buf.data() + o + 17 * N, 4 * N);
+    if (rc) { destroy_handle(h); return rc; }
+    *cfg = c;
+    *out = h;
+    return ION_OK;
+}
+
+// ---- timing ------------------------------------------------------------------
+int ion_lbm_record_event(ion_lbm* h, int slot) {
+    if (!h || slot < 0 || slot >= 8) return fail(ION_E_INVALID, "bad event slot");
+    CK(cudaEventRecord(h->ev[slot], h->stream));
+    return ION_OK;
+}
+
+int ion_lbm_event_elapsed(ion_lbm* h, int a, int b, float* ms) {
+    if (!h || !ms || a < 0 || a >= 8 || b < 0 || b >= 8) return fail(ION_E_INVALID, "bad event slot");
+    CK(cudaEventSynchronize(h->ev[b]));
+    CK(cudaEventElapsedTime(ms, h->ev[a], h->ev[b]));
+    return ION_OK;
+}
+
+int ion_lbm_set_kernel_timing(ion_lbm* h, int enable) {
+    if (!h) return fail(ION_E_INVALID, "null handle");
+    h->ktiming = enable != 0;
+    return ION_OK;
+}
+
+int ion_lbm_kernel_time(ion_lbm* h, int kernel, double* total_ms, uint64_t* launches) {
+    if (!h || kernel < 0 || kernel > 2) return fail(ION_E_INVALID, "bad kernel id");
+    if (!h->kev.empty()) {
+        CK(cudaStreamSynchronize(h->stream));
+        for (auto& e : h->kev) {
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, e.a, e.b));
+            h->ktime[e.kernel] += ms;
+            h->kcount[e.kernel] += 1;
+            h->ev_pool.push_back(e.a);
+            h->ev_pool.push_back(e.b);
+        }
+        h->kev.clear();
+    }
+    if (total_ms) *total_ms = h->ktime[kernel];
+    if (launches) *launches = h->kcount[kernel];
+    return ION_OK;
+}
+
+int ion_lbm_reset_kernel_time(ion_lbm* h) {
+    if (!h) return fail(ION_E_INVALID, "null handle");
+    double d;
+    uint64_t c;
+    int rc = ion_lbm_kernel_time(h, 0, &d, &c);
+    if (rc) return rc;
+    for (int i = 0; i < 3; i++) { h->ktime[i] = 0; h->kcount[i] = 0; }
+    return ION_OK;
+}
+
+// ---- device selection and the FP32 peak probe ---------------------------------
+int ion_select_device(int device) {
+    CK(cudaSetDevice(device));
+    return ION_OK;
+}
+
+int ion_probe_fp32_peak(double* tflops) {
+    if (!tflops) return fail(ION_E_INVALID, "null argument");
+    int dev = 0, sms = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    float* out = nullptr;
+    CK(cudaMalloc(&out, 1024 * sizeof(float)));
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const int blocks = sms * 8, iters = 1 << 16;
+    launch_fma_probe(out, blocks, 1024, 0);  // warm-up
+    cudaEventRecord(a, 0);
+    launch_fma_probe(out, blocks, iters, 0);
+    cudaEventRecord(b, 0);
+    g_launches += 2;
+    cudaError_t e = cudaEventSynchronize(b);
+    float ms = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(out);
+    if (e != cudaSuccess) return fail(ION_E_CUDA, "fma probe: %s", cudaGetErrorString(e));
+    const double flops = 2.0 * 8.0 * (double)iters * 256.0 * (double)blocks;  // FMA = 2 FLOP
+    *tflops = flops / (ms * 1e-3) / 1e12;
+    return ION_OK;
+}
+
+// ---- device codec check -------------------------------------------------------
+int ion_codec_roundtrip(int float_type, const float* in, uint16_t* enc, float* dec, const uint16_t* raw, float* raw_dec,
+                        uint64_t n) {
+    if (float_type != ION_FP16S && float_type != ION_FP16C) return fail(ION_E_INVALID, "codec must be FP16S or FP16C");
+    if (!n) return ION_OK;
+    float *d_in = nullptr, *d_dec = nullptr, *d_rdec = nullptr;
+    uint16_t *d_enc = nullptr, *d_raw = nullptr;
+    int rc = ION_OK;
+    if (cudaMalloc(&d_in, n * 4) != cudaSuccess || cudaMalloc(&d_dec, n * 4) != cudaSuccess ||
+        cudaMalloc(&d_rdec, n * 4) != cudaSuccess || cudaMalloc(&d_enc, n * 2) != cudaSuccess ||
+        cudaMalloc(&d_raw, n * 2) != cudaSuccess) {
+        rc = fail(ION_E_NOMEM, "codec buffers");
+    } else {
+        cudaMemcpy(d_in, in, n * 4, cudaMemcpyHostToDevice);
+        cudaMemcpy(d_raw, raw, n * 2, cudaMemcpyHostToDevice);
+        launch_codec(float_type, d_in, d_enc, d_dec, d_raw, d_rdec, n, 0);
+        g_launches++;
+        if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = fail(ION_E_CUDA, "codec kernel");
+        cudaMemcpy(enc, d_enc, n * 2, cudaMemcpyDeviceToHost);
+        cudaMemcpy(dec, d_dec, n * 4, cudaMemcpyDeviceToHost);
+        cudaMemcpy(raw_dec, d_rdec, n * 4, cudaMemcpyDeviceToHost);
+    }
+    cudaFree(d_in); cudaFree(d_dec); cudaFree(d_rdec); cudaFree(d_enc); cudaFree(d_raw);
+    return rc;
+}
+
+}  // extern "C"

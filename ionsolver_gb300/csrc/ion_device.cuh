@@ -1,0 +1,190 @@
+// ion_device.cuh -- shared device-side definitions of the GB300 MHD-LBM path.
+//
+// Everything here is compiled with -fmad=false: a*b+c stays two IEEE
+// roundings unless the code calls fmaf(), which is how the reference's
+// kernels are written (IonSolver src/kernels/sim_kernels.cl).  Division and
+// sqrt are the IEEE round-to-nearest ones (-prec-div=true -prec-sqrt=true).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+
+#include "ionsolver.h"
+
+namespace ion {
+
+// flag bits, IonSolver src/lbm/domain.rs:819-828
+constexpr uint8_t F_S = 0x01, F_E = 0x02, F_C = 0x04, F_F = 0x08, F_M = 0x10, F_BO = 0x1F;
+
+// lattice speed of sound c = 1/sqrt(3) as the literal DEF_C (domain.rs:807)
+constexpr float CS = 0.57735027f;
+constexpr float THIRD = 0.33333334f;  // literal of sim_kernels.cl:369-375
+
+// ---------------------------------------------------------------------------
+// Velocity sets (directions in +/- pairs; order of sim_kernels.cl:326-347).
+// ---------------------------------------------------------------------------
+template <int Q> struct VSet;
+
+template <> struct VSet<19> {
+    static constexpr int q = 19, dims = 3;
+    __host__ __device__ static constexpr int c(int i, int a) {
+        constexpr int8_t t[19][3] = {{0,0,0},{1,0,0},{-1,0,0},{0,1,0},{0,-1,0},{0,0,1},{0,0,-1},{1,1,0},{-1,-1,0},
+                                     {1,0,1},{-1,0,-1},{0,1,1},{0,-1,-1},{1,-1,0},{-1,1,0},{1,0,-1},{-1,0,1},
+                                     {0,1,-1},{0,-1,1}};
+        return t[i][a];
+    }
+    __host__ __device__ static constexpr int wc(int i) { return i == 0 ? 0 : (i < 7 ? 1 : 2); }
+    // DEF_W0/WS/WE of get_device_defines (domain.rs:763-765)
+    __host__ __device__ static constexpr float w(int k) { return k == 0 ? (1.0f / 3.0f) : k == 1 ? (1.0f / 18.0f) : (1.0f / 36.0f); }
+};
+
+template <> struct VSet<15> {
+    static constexpr int q = 15, dims = 3;
+    __host__ __device__ static constexpr int c(int i, int a) {
+        constexpr int8_t t[15][3] = {{0,0,0},{1,0,0},{-1,0,0},{0,1,0},{0,-1,0},{0,0,1},{0,0,-1},{1,1,1},{-1,-1,-1},
+                                     {1,1,-1},{-1,-1,1},{1,-1,1},{-1,1,-1},{-1,1,1},{1,-1,-1}};
+        return t[i][a];
+    }
+    __host__ __device__ static constexpr int wc(int i) { return i == 0 ? 0 : (i < 7 ? 1 : 2); }
+    __host__ __device__ static constexpr float w(int k) { return k == 0 ? (1.0f / 4.5f) : k == 1 ? (1.0f / 9.0f) : (1.0f / 72.0f); }
+};
+
+template <> struct VSet<9> {
+    static constexpr int q = 9, dims = 2;
+    __host__ __device__ static constexpr int c(int i, int a) {
+        constexpr int8_t t[9][3] = {{0,0,0},{1,0,0},{-1,0,0},{0,1,0},{0,-1,0},{1,1,0},{-1,-1,0},{1,-1,0},{-1,1,0}};
+        return t[i][a];
+    }
+    __host__ __device__ static constexpr int wc(int i) { return i == 0 ? 0 : (i < 5 ? 1 : 2); }
+    __host__ __device__ static constexpr float w(int k) { return k == 0 ? (1.0f / 2.25f) : k == 1 ? (1.0f / 9.0f) : (1.0f / 36.0f); }
+};
+
+// ---------------------------------------------------------------------------
+// 32-bit unsigned division by a runtime-invariant divisor (Granlund &
+// Montgomery, "Division by invariant integers using multiplication", 1994,
+// round-up variant with a 33-bit intermediate): q = (umulhi(n,m) + n) >> l.
+// ---------------------------------------------------------------------------
+struct FastDiv {
+    uint32_t d, m, l;
+    FastDiv() : d(1), m(1), l(0) {}
+    explicit FastDiv(uint32_t div) : d(div) {
+        l = 0;
+        while ((1ull << l) < div) l++;
+        m = (uint32_t)((((1ull << 32) * ((1ull << l) - div)) / div) + 1ull);
+    }
+    __host__ __device__ __forceinline__ uint32_t div(uint32_t n) const {
+#ifdef __CUDA_ARCH__
+        const uint32_t t = __umulhi(n, m);
+#else
+        const uint32_t t = (uint32_t)(((uint64_t)n * m) >> 32);
+#endif
+        return (uint32_t)(((uint64_t)t + n) >> l);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// DDF storage codecs.
+//   FP32 : plain float.
+//   FP16S: IEEE binary16 of x*2^15, round to nearest even
+//          (vstore_half_rte / vload_half, domain.rs:773-776).
+//   FP16C: the reference's 1-4-11 format (sim_kernels.cl:79-90): the float's
+//          bit pattern plus 2^11, 4 exponent bits (bias 15), 11 mantissa bits.
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ uint32_t fbits(float f) {
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(f);
+#else
+    uint32_t u; __builtin_memcpy(&u, &f, 4); return u;
+#endif
+}
+__host__ __device__ __forceinline__ float bitsf(uint32_t u) {
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    float f; __builtin_memcpy(&f, &u, 4); return f;
+#endif
+}
+
+__host__ __device__ __forceinline__ uint16_t fp16c_encode(float x) {
+    const uint32_t b = fbits(x) + 0x800u;
+    const uint32_t e = (b & 0x7F800000u) >> 23, m = b & 0x007FFFFFu;
+    uint32_t out = (b & 0x80000000u) >> 16;
+    if (e > 112u) out |= (((e - 112u) << 11) & 0x7800u) | (m >> 12);
+    else if (e > 100u) out |= (((0x007FF800u + m) >> (124u - e)) + 1u) >> 1;
+    return (uint16_t)out;
+}
+__host__ __device__ __forceinline__ float fp16c_decode(uint16_t x) {
+    const uint32_t e = (x & 0x7800u) >> 11, m = (uint32_t)(x & 0x07FFu) << 12;
+    uint32_t out = (uint32_t)(x & 0x8000u) << 16;
+    if (e != 0u) {
+        out |= ((e + 112u) << 23) | m;
+    } else if (m != 0u) {
+#ifdef __CUDA_ARCH__
+        const uint32_t lead = 31u - (uint32_t)__clz(m);
+#else
+        const uint32_t lead = 31u - (uint32_t)__builtin_clz(m);
+#endif
+        out |= ((lead + 90u) << 23) | ((m << (23u - lead)) & 0x007FF000u);
+    }
+    return bitsf(out);
+}
+
+template <int FT> struct Ddf;
+template <> struct Ddf<ION_FP32> {
+    using T = float;
+    __device__ __forceinline__ static float ld(const float* p, size_t i) { return p[i]; }
+    __device__ __forceinline__ static void st(float* p, size_t i, float x) { p[i] = x; }
+};
+template <> struct Ddf<ION_FP16S> {
+    using T = uint16_t;
+    __device__ __forceinline__ static float ld(const uint16_t* p, size_t i) {
+        return __half2float(__ushort_as_half(p[i])) * 3.0517578E-5f;
+    }
+    __device__ __forceinline__ static void st(uint16_t* p, size_t i, float x) {
+        p[i] = __half_as_ushort(__float2half_rn(x * 32768.0f));
+    }
+};
+template <> struct Ddf<ION_FP16C> {
+    using T = uint16_t;
+    __device__ __forceinline__ static float ld(const uint16_t* p, size_t i) { return fp16c_decode(p[i]); }
+    __device__ __forceinline__ static void st(uint16_t* p, size_t i, float x) { p[i] = fp16c_encode(x); }
+};
+
+// ---------------------------------------------------------------------------
+// Device view of one domain (all pointers are device memory).
+// ---------------------------------------------------------------------------
+struct DevLbm {
+    uint32_t nx, ny, nz;
+    uint32_t n;            // cells (< 2^32, as the reference's uint n)
+    FastDiv dx, dxy;       // divisions by nx and nx*ny
+    void* fi;              // [q][N]
+    float* rho;            // [N]
+    float* u;              // [3][N]
+    uint8_t* flags;        // [N]
+    float* F;              // [3][N] or null
+    float *e_stat, *b_stat, *e_dyn, *b_dyn;  // [3][N]
+    void* fqi;             // [7][N]
+    void* ei;              // [q][N]
+    float* q;              // [N]
+    float* qu_lod;         // [n_lod][4]
+    float* lod_cell;       // scratch [3][N]: u*ils per cell for the LOD sums
+    float4* lod_pos;       // [n_lod_own] LOD bin centres
+    float w, ke, kmu, kmu0, kkge, wq;
+    float fx, fy, fz;
+    uint32_t depth, nd, n_lod_own, n_bins, first_src;
+    uint32_t bsx, bsy, bsz;      // LOD bin extent in cells
+    uint32_t near_x, near_y, near_z;  // near-field block extent
+    float ils;
+    uint8_t ext_eq, ext_vf, ext_ff, ext_mhd, update_fields;
+};
+
+__device__ __forceinline__ void cell_xyz(const DevLbm& L, uint32_t n, uint32_t& x, uint32_t& y, uint32_t& z) {
+    z = L.dxy.div(n);
+    const uint32_t r = n - z * L.nx * L.ny;
+    y = L.dx.div(r);
+    x = r - y * L.nx;
+}
+
+__device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+
+}  // namespace ion

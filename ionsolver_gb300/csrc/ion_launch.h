@@ -1,0 +1,49 @@
+// ion_launch.h -- host-side launchers of the sm_103a kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ion {
+
+struct DevLbm;
+
+inline unsigned grid_for(uint64_t n, unsigned block) {
+    const uint64_t g = (n + block - 1) / block;
+    return (unsigned)(g ? g : 1);
+}
+
+// voxelize_mesh arguments (IonSolver src/mesh.rs:281-343)
+struct VoxArgs {
+    const float *p0, *p1, *p2;  // device, [ntri][3]
+    uint32_t ntri;
+    int direction;
+    uint32_t columns;
+    float x0, y0, z0, x1, y1, z1;  // bounding box +-2
+    uint8_t flag;
+    float mx, my, mz;
+};
+
+constexpr unsigned RED_BLOCK = 256;
+
+// per velocity set (lbm_q19.cu, lbm_q15.cu, lbm_q9.cu)
+#define ION_DECLARE_LBM_DISPATCH(NAME)                                                                    \
+    void NAME##_stream_collide(const DevLbm& L, int ft, bool mhd, bool trt, uint64_t t, cudaStream_t s);  \
+    void NAME##_initialize(const DevLbm& L, int ft, bool mhd, cudaStream_t s);                            \
+    void NAME##_update_fields(const DevLbm& L, int ft, uint64_t t, cudaStream_t s);
+ION_DECLARE_LBM_DISPATCH(q19)
+ION_DECLARE_LBM_DISPATCH(q15)
+ION_DECLARE_LBM_DISPATCH(q9)
+
+void launch_lod_bins(const DevLbm& L, cudaStream_t s);
+void launch_update_e_b(const DevLbm& L, bool fast, uint32_t* err, cudaStream_t s);
+void launch_voxelize(const DevLbm& L, const VoxArgs& A, cudaStream_t s);
+void launch_compact(const DevLbm& L, uint8_t mask, uint32_t* tiles, uint32_t* list, uint32_t* total, cudaStream_t s);
+void launch_psi_static_b(const DevLbm& L, const uint32_t* mags, const uint32_t* count, cudaStream_t s);
+void launch_static_e(const DevLbm& L, const uint32_t* list, const uint32_t* count, cudaStream_t s);
+void launch_sum_f64(const void* x, int ft, uint64_t count, double* partials, uint32_t nparts, double* out,
+                    cudaStream_t s);
+void launch_fma_probe(float* out, int blocks, int iters, cudaStream_t s);
+void launch_codec(int ft, const float* in, uint16_t* enc, float* dec, const uint16_t* raw, float* raw_dec, uint64_t n,
+                  cudaStream_t s);
+
+}  // namespace ion

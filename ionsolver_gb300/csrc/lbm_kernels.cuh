@@ -1,0 +1,377 @@
+// lbm_kernels.cuh -- initialize / stream_collide / update_fields of the
+// IonSolver timestep as sm_103a kernels (one thread per cell, grid-stride).
+//
+// Per cell the arithmetic follows the reference kernel operation for
+// operation (IonSolver src/kernels/sim_kernels.cl:465-859), so results are
+// bit-identical to it when it runs in cell order; with -fmad=false no
+// product is fused unless the reference calls fma().  The one structural
+// change is the LOD accumulation (sim_kernels.cl:666-677): instead of four
+// float atomics per cell, each cell stores its velocity contribution and a
+// separate pass (field_kernels.cu) sums every bin in ascending cell order.
+#pragma once
+#include "ion_device.cuh"
+#include "ion_launch.h"
+
+namespace ion {
+
+// Esoteric-Pull neighbour index for direction i (periodic, sim_kernels.cl:248-302)
+struct Nbr {
+    uint32_t x0, xp, xm, y0, yp, ym, z0, zp, zm;  // x, and y*nx / z*nx*ny offsets
+    __device__ __forceinline__ Nbr(const DevLbm& L, uint32_t x, uint32_t y, uint32_t z) {
+        const uint32_t nxy = L.nx * L.ny;
+        x0 = x; xp = (x + 1u == L.nx) ? 0u : x + 1u; xm = (x == 0u) ? L.nx - 1u : x - 1u;
+        y0 = y * L.nx; yp = ((y + 1u == L.ny) ? 0u : y + 1u) * L.nx; ym = ((y == 0u) ? L.ny - 1u : y - 1u) * L.nx;
+        z0 = z * nxy; zp = ((z + 1u == L.nz) ? 0u : z + 1u) * nxy; zm = ((z == 0u) ? L.nz - 1u : z - 1u) * nxy;
+    }
+    template <class V>
+    __device__ __forceinline__ uint32_t operator()(int i) const {
+        const int cx = V::c(i, 0), cy = V::c(i, 1), cz = V::c(i, 2);
+        return (cx > 0 ? xp : cx < 0 ? xm : x0) + (cy > 0 ? yp : cy < 0 ? ym : y0) + (cz > 0 ? zp : cz < 0 ? zm : z0);
+    }
+};
+
+// density / velocity from DDF-shifted populations (sim_kernels.cl:208-233)
+template <class V>
+__device__ __forceinline__ void moments(const float* f, float& rho, float& ux, float& uy, float& uz) {
+    float r = f[0];
+#pragma unroll
+    for (int i = 1; i < V::q; i++) r = r + f[i];
+    r = r + 1.0f;
+    float u[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        bool first = true;
+        float acc = 0.0f;
+#pragma unroll
+        for (int i = 1; i < V::q; i += 2) {
+            const int s = V::c(i, a);
+            if (s == 0) continue;
+            const float pos = s > 0 ? f[i] : f[i + 1], neg = s > 0 ? f[i + 1] : f[i];
+            acc = first ? pos - neg : (acc + pos) - neg;
+            first = false;
+        }
+        u[a] = acc;
+    }
+    rho = r;
+    ux = u[0] / r;
+    uy = u[1] / r;
+    uz = (V::dims == 2 ? 0.0f : u[2]) / r;
+}
+
+// c_i . v over the non-zero components in x,y,z order (sim_kernels.cl:162-205)
+template <class V>
+__device__ __forceinline__ float project(int i, float vx, float vy, float vz) {
+    bool first = true;
+    float acc = 0.0f;
+    const float comp[3] = {vx, vy, vz};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int s = V::c(i, a);
+        if (s == 0) continue;
+        if (first) { acc = s > 0 ? comp[a] : -comp[a]; first = false; }
+        else acc = s > 0 ? acc + comp[a] : acc - comp[a];
+    }
+    return acc;
+}
+
+// equilibrium, DDF-shifted (sim_kernels.cl:155-207)
+template <class V>
+__device__ __forceinline__ void equilibrium(float rho, float ux, float uy, float uz, float* feq) {
+    const float c3 = -3.0f * ((ux * ux + uy * uy) + uz * uz), rm1 = rho - 1.0f;
+    ux = ux * 3.0f; uy = uy * 3.0f; uz = uz * 3.0f;
+    feq[0] = V::w(0) * fmaf(rho, 0.5f * c3, rm1);
+#pragma unroll
+    for (int i = 1; i < V::q; i += 2) {
+        const float wr = V::w(V::wc(i)) * rho, wrm1 = V::w(V::wc(i)) * rm1;
+        const float p = project<V>(i, ux, uy, uz);
+        feq[i] = fmaf(wr, fmaf(0.5f, fmaf(p, p, c3), p), wrm1);
+        feq[i + 1] = fmaf(wr, fmaf(0.5f, fmaf(p, p, c3), -p), wrm1);
+    }
+}
+
+// Guo forcing terms (sim_kernels.cl:367-377)
+template <class V>
+__device__ __forceinline__ void forcing(float ux, float uy, float uz, float fx, float fy, float fz, float* Fin) {
+    const float uF = V::dims == 2 ? -THIRD * fmaf(ux, fx, uy * fy) : -THIRD * fmaf(ux, fx, fmaf(uy, fy, uz * fz));
+    Fin[0] = (9.0f * V::w(0)) * uF;
+#pragma unroll
+    for (int i = 1; i < V::q; i++) {
+        const float cx = (float)V::c(i, 0), cy = (float)V::c(i, 1), cz = (float)V::c(i, 2);
+        const float cf = (cx * fx + cy * fy) + cz * fz;
+        const float cu = ((cx * ux + cy * uy) + cz * uz) + THIRD;
+        Fin[i] = (9.0f * V::w(V::wc(i))) * fmaf(cf, cu, uF);
+    }
+}
+
+// D3Q7 advection equilibrium (sim_kernels.cl:390-396)
+__device__ __forceinline__ void adv_equilibrium(float Q, float ux, float uy, float uz, float* a) {
+    const float hq = 0.5f * Q, eq = 0.125f * (Q - 1.0f);
+    a[0] = fmaf(0.25f, Q, -0.25f);
+    a[1] = fmaf(hq, ux, eq); a[2] = fmaf(hq, -ux, eq);
+    a[3] = fmaf(hq, uy, eq); a[4] = fmaf(hq, -uy, eq);
+    a[5] = fmaf(hq, uz, eq); a[6] = fmaf(hq, -uz, eq);
+}
+
+// Esoteric-Pull load/store (sim_kernels.cl:234-247, 397-410)
+template <class D, int Q, class NB>
+__device__ __forceinline__ void ep_load(const typename D::T* f, uint32_t N, uint32_t n, bool odd, const NB& j, float* v) {
+    v[0] = D::ld(f, n);
+#pragma unroll
+    for (int i = 1; i < Q; i += 2) {
+        v[i] = D::ld(f, (size_t)(odd ? i : i + 1) * N + n);
+        v[i + 1] = D::ld(f, (size_t)(odd ? i + 1 : i) * N + j(i));
+    }
+}
+template <class D, int Q, class NB>
+__device__ __forceinline__ void ep_store(typename D::T* f, uint32_t N, uint32_t n, bool odd, const NB& j, const float* v) {
+    D::st(f, n, v[0]);
+#pragma unroll
+    for (int i = 1; i < Q; i += 2) {
+        D::st(f, (size_t)(odd ? i + 1 : i) * N + j(i), v[i]);
+        D::st(f, (size_t)(odd ? i : i + 1) * N + n, v[i + 1]);
+    }
+}
+
+template <class V>
+struct NbV {  // neighbour functor of a velocity set
+    const Nbr& b;
+    __device__ __forceinline__ uint32_t operator()(int i) const { return b.template operator()<V>(i); }
+};
+struct Nb7 {  // D3Q7 subset (sim_kernels.cl:382-389)
+    const Nbr& b;
+    __device__ __forceinline__ uint32_t operator()(int i) const {
+        return i == 1 ? b.xp + b.y0 + b.z0 : i == 3 ? b.x0 + b.yp + b.z0 : b.x0 + b.y0 + b.zp;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// stream_collide, one step (sim_kernels.cl:465-758)
+// ---------------------------------------------------------------------------
+template <int Q, int FT, bool MHD, bool TRT>
+__global__ void __launch_bounds__(256) k_stream_collide(const DevLbm L, const uint32_t odd_t) {
+    using V = VSet<Q>;
+    using D = Ddf<FT>;
+    using T = typename D::T;
+    const uint32_t N = L.n;
+    const bool odd = odd_t != 0u;
+    for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        const uint8_t fbo = L.flags[n] & F_BO;
+        if (fbo == F_S) continue;
+        const bool eqc = L.ext_eq && fbo == F_E;
+        uint32_t x, y, z;
+        cell_xyz(L, n, x, y, z);
+        const Nbr nb(L, x, y, z);
+        const NbV<V> j{nb};
+        float fhn[Q], feq[Q], Fin[Q];
+        ep_load<D, Q>((const T*)L.fi, N, n, odd, j, fhn);
+        float rhon, uxn, uyn, uzn;
+        if (eqc) { rhon = L.rho[n]; uxn = L.u[n]; uyn = L.u[(size_t)N + n]; uzn = L.u[2 * (size_t)N + n]; }
+        else moments<V>(fhn, rhon, uxn, uyn, uzn);
+
+        float fxn = L.fx, fyn = L.fy, fzn = L.fz;
+        const float w = L.w;
+        const float c_tau = fmaf(w, -0.5f, 1.0f);
+        if (L.ext_ff) { fxn = fxn + L.F[n]; fyn = fyn + L.F[(size_t)N + n]; fzn = fzn + L.F[2 * (size_t)N + n]; }
+
+        if constexpr (MHD) {
+            const float Bx = L.b_dyn[n], By = L.b_dyn[(size_t)N + n], Bz = L.b_dyn[2 * (size_t)N + n];
+            const float Ex = L.e_dyn[n], Ey = L.e_dyn[(size_t)N + n], Ez = L.e_dyn[2 * (size_t)N + n];
+            // electron gas, part 1
+            float ehn[Q];
+            ep_load<D, Q>((const T*)L.ei, N, n, odd, j, ehn);
+            float rhoe, uxe, uye, uze;
+            moments<V>(ehn, rhoe, uxe, uye, uze);
+            // charge advection (D3Q7)
+            const Nb7 j7{nb};
+            float qhn[7];
+            ep_load<D, 7>((const T*)L.fqi, N, n, odd, j7, qhn);
+            float rhoq = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 7; i++) rhoq = rhoq + qhn[i];
+            rhoq = rhoq + 1.0f;
+            L.q[n] = rhoq - rhoe;
+            float aeq[7];
+            adv_equilibrium(rhoq, uxn, uyn, uzn, aeq);
+#pragma unroll
+            for (int i = 0; i < 7; i++) qhn[i] = fmaf(1.0f - L.wq, qhn[i], L.wq * aeq[i]);
+            ep_store<D, 7>((T*)L.fqi, N, n, odd, j7, qhn);
+            // electron gas, part 2: Lorentz force, Guo half-step, SRT
+            const float cxv = uye * Bz - uze * By, cyv = uze * Bx - uxe * Bz, czv = uxe * By - uye * Bx;
+            const float nre = -rhoe;
+            const float efx = nre * (Ex + cxv), efy = nre * (Ey + cyv), efz = nre * (Ez + czv);
+            const float r2e = 0.5f / (rhoe * L.kkge);
+            uxe = clampf(fmaf(efx, r2e, uxe), -CS, CS);
+            uye = clampf(fmaf(efy, r2e, uye), -CS, CS);
+            uze = clampf(fmaf(efz, r2e, uze), -CS, CS);
+            forcing<V>(uxe, uye, uze, efx, efy, efz, Fin);
+            equilibrium<V>(rhoe, uxe, uye, uze, feq);
+#pragma unroll
+            for (int i = 0; i < Q; i++) Fin[i] = Fin[i] * c_tau;
+#pragma unroll
+            for (int i = 0; i < Q; i++) ehn[i] = eqc ? feq[i] : fmaf(1.0f - w, ehn[i], fmaf(w, feq[i], Fin[i]));
+            ep_store<D, Q>((T*)L.ei, N, n, odd, j, ehn);
+            // Lorentz force on the gas
+            fxn = fxn + rhoq * ((Ex + uyn * Bz) - uzn * By);
+            fyn = fyn + rhoq * ((Ey + uzn * Bx) - uxn * Bz);
+            fzn = fzn + rhoq * ((Ez + uxn * By) - uyn * Bx);
+            // LOD contribution: velocity / bin volume (charge is q[n])
+            if (L.depth > 0u) {
+                L.lod_cell[n] = uxn * L.ils;
+                L.lod_cell[(size_t)N + n] = uyn * L.ils;
+                L.lod_cell[2 * (size_t)N + n] = uzn * L.ils;
+            }
+        }
+
+        if (L.ext_vf) {
+            const float r2 = 0.5f / rhon;
+            uxn = clampf(fmaf(fxn, r2, uxn), -CS, CS);
+            uyn = clampf(fmaf(fyn, r2, uyn), -CS, CS);
+            uzn = clampf(fmaf(fzn, r2, uzn), -CS, CS);
+            forcing<V>(uxn, uyn, uzn, fxn, fyn, fzn, Fin);
+        } else {
+            uxn = clampf(uxn, -CS, CS);
+            uyn = clampf(uyn, -CS, CS);
+            uzn = clampf(uzn, -CS, CS);
+#pragma unroll
+            for (int i = 0; i < Q; i++) Fin[i] = 0.0f;
+        }
+        if (L.update_fields && !eqc) {
+            L.rho[n] = rhon;
+            L.u[n] = uxn; L.u[(size_t)N + n] = uyn; L.u[2 * (size_t)N + n] = uzn;
+        }
+        equilibrium<V>(rhon, uxn, uyn, uzn, feq);
+        if constexpr (TRT) {
+            const float wp = w, wm = 1.0f / (0.1875f / (1.0f / w - 0.5f) + 0.5f);
+            if (L.ext_vf) {
+                const float ctp = fmaf(wp, -0.25f, 0.5f), ctm = fmaf(wm, -0.25f, 0.5f);
+                float Fb[Q];
+                Fb[0] = Fin[0];
+#pragma unroll
+                for (int i = 1; i < Q; i += 2) { Fb[i] = Fin[i + 1]; Fb[i + 1] = Fin[i]; }
+#pragma unroll
+                for (int i = 0; i < Q; i++) Fin[i] = fmaf(ctp, Fin[i] + Fb[i], ctm * (Fin[i] - Fb[i]));
+            }
+            float fb[Q], eb[Q];
+            fb[0] = fhn[0]; eb[0] = feq[0];
+#pragma unroll
+            for (int i = 1; i < Q; i += 2) { fb[i] = fhn[i + 1]; fb[i + 1] = fhn[i]; eb[i] = feq[i + 1]; eb[i + 1] = feq[i]; }
+#pragma unroll
+            for (int i = 0; i < Q; i++) {
+                const float sym = ((feq[i] - fhn[i]) + eb[i]) - fb[i];
+                const float asym = ((feq[i] - eb[i]) - fhn[i]) + fb[i];
+                fhn[i] = eqc ? feq[i] : fmaf(0.5f * wp, sym, fmaf(0.5f * wm, asym, fhn[i] + Fin[i]));
+            }
+        } else {
+            if (L.ext_vf) {
+#pragma unroll
+                for (int i = 0; i < Q; i++) Fin[i] = Fin[i] * c_tau;
+            }
+#pragma unroll
+            for (int i = 0; i < Q; i++) fhn[i] = eqc ? feq[i] : fmaf(1.0f - w, fhn[i], fmaf(w, feq[i], Fin[i]));
+        }
+        ep_store<D, Q>((T*)L.fi, N, n, odd, j, fhn);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// initialize (sim_kernels.cl:760-832): equilibrium DDFs stored with parity 1
+// ---------------------------------------------------------------------------
+template <int Q, int FT, bool MHD>
+__global__ void __launch_bounds__(256) k_initialize(const DevLbm L) {
+    using V = VSet<Q>;
+    using D = Ddf<FT>;
+    using T = typename D::T;
+    const uint32_t N = L.n;
+    for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        uint32_t x, y, z;
+        cell_xyz(L, n, x, y, z);
+        const Nbr nb(L, x, y, z);
+        const NbV<V> j{nb};
+        if ((L.flags[n] & F_BO) == F_S) {
+            L.u[n] = 0.0f; L.u[(size_t)N + n] = 0.0f; L.u[2 * (size_t)N + n] = 0.0f;
+            if constexpr (MHD) L.q[n] = 0.0f;
+        }
+        const float ux = L.u[n], uy = L.u[(size_t)N + n], uz = L.u[2 * (size_t)N + n];
+        float feq[Q];
+        equilibrium<V>(L.rho[n], ux, uy, uz, feq);
+        ep_store<D, Q>((T*)L.fi, N, n, true, j, feq);
+        if constexpr (MHD) {
+            float aeq[7];
+            adv_equilibrium(L.q[n], ux, uy, uz, aeq);
+            const Nb7 j7{nb};
+            ep_store<D, 7>((T*)L.fqi, N, n, true, j7, aeq);
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                L.b_dyn[(size_t)c * N + n] = L.b_stat[(size_t)c * N + n];
+                L.e_dyn[(size_t)c * N + n] = L.e_stat[(size_t)c * N + n];
+            }
+            equilibrium<V>(0.0f, ux, uy, uz, feq);
+            ep_store<D, Q>((T*)L.ei, N, n, true, j, feq);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// update_fields (sim_kernels.cl:834-859)
+// ---------------------------------------------------------------------------
+template <int Q, int FT>
+__global__ void __launch_bounds__(256) k_update_fields(const DevLbm L, const uint32_t odd_t) {
+    using V = VSet<Q>;
+    using D = Ddf<FT>;
+    using T = typename D::T;
+    const uint32_t N = L.n;
+    for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        if ((L.flags[n] & F_BO) == F_S) continue;
+        uint32_t x, y, z;
+        cell_xyz(L, n, x, y, z);
+        const Nbr nb(L, x, y, z);
+        const NbV<V> j{nb};
+        float f[Q], rho, ux, uy, uz;
+        ep_load<D, Q>((const T*)L.fi, N, n, odd_t != 0u, j, f);
+        moments<V>(f, rho, ux, uy, uz);
+        L.rho[n] = rho;
+        L.u[n] = clampf(ux, -CS, CS);
+        L.u[(size_t)N + n] = clampf(uy, -CS, CS);
+        L.u[2 * (size_t)N + n] = clampf(uz, -CS, CS);
+    }
+}
+
+#define ION_DEFINE_LBM_DISPATCH(QV, NAME)                                                                     \
+    void NAME##_stream_collide(const DevLbm& L, int ft, bool mhd, bool trt, uint64_t t, cudaStream_t s) {      \
+        const unsigned g = grid_for(L.n, 256);                                                                 \
+        const uint32_t o = (uint32_t)(t & 1u);                                                                 \
+        if (ft == ION_FP32) {                                                                                  \
+            if (mhd) { if (trt) k_stream_collide<QV, ION_FP32, true, true><<<g, 256, 0, s>>>(L, o);            \
+                       else k_stream_collide<QV, ION_FP32, true, false><<<g, 256, 0, s>>>(L, o); }             \
+            else { if (trt) k_stream_collide<QV, ION_FP32, false, true><<<g, 256, 0, s>>>(L, o);               \
+                   else k_stream_collide<QV, ION_FP32, false, false><<<g, 256, 0, s>>>(L, o); }                \
+        } else if (ft == ION_FP16S) {                                                                          \
+            if (mhd) { if (trt) k_stream_collide<QV, ION_FP16S, true, true><<<g, 256, 0, s>>>(L, o);           \
+                       else k_stream_collide<QV, ION_FP16S, true, false><<<g, 256, 0, s>>>(L, o); }            \
+            else { if (trt) k_stream_collide<QV, ION_FP16S, false, true><<<g, 256, 0, s>>>(L, o);              \
+                   else k_stream_collide<QV, ION_FP16S, false, false><<<g, 256, 0, s>>>(L, o); }               \
+        } else {                                                                                               \
+            if (mhd) { if (trt) k_stream_collide<QV, ION_FP16C, true, true><<<g, 256, 0, s>>>(L, o);           \
+                       else k_stream_collide<QV, ION_FP16C, true, false><<<g, 256, 0, s>>>(L, o); }            \
+            else { if (trt) k_stream_collide<QV, ION_FP16C, false, true><<<g, 256, 0, s>>>(L, o);              \
+                   else k_stream_collide<QV, ION_FP16C, false, false><<<g, 256, 0, s>>>(L, o); }               \
+        }                                                                                                      \
+    }                                                                                                          \
+    void NAME##_initialize(const DevLbm& L, int ft, bool mhd, cudaStream_t s) {                                \
+        const unsigned g = grid_for(L.n, 256);                                                                 \
+        if (ft == ION_FP32) { if (mhd) k_initialize<QV, ION_FP32, true><<<g, 256, 0, s>>>(L);                  \
+                              else k_initialize<QV, ION_FP32, false><<<g, 256, 0, s>>>(L); }                   \
+        else if (ft == ION_FP16S) { if (mhd) k_initialize<QV, ION_FP16S, true><<<g, 256, 0, s>>>(L);           \
+                                    else k_initialize<QV, ION_FP16S, false><<<g, 256, 0, s>>>(L); }            \
+        else { if (mhd) k_initialize<QV, ION_FP16C, true><<<g, 256, 0, s>>>(L);                                \
+               else k_initialize<QV, ION_FP16C, false><<<g, 256, 0, s>>>(L); }                                 \
+    }                                                                                                          \
+    void NAME##_update_fields(const DevLbm& L, int ft, uint64_t t, cudaStream_t s) {                           \
+        const unsigned g = grid_for(L.n, 256);                                                                 \
+        const uint32_t o = (uint32_t)(t & 1u);                                                                 \
+        if (ft == ION_FP32) k_update_fields<QV, ION_FP32><<<g, 256, 0, s>>>(L, o);                             \
+        else if (ft == ION_FP16S) k_update_fields<QV, ION_FP16S><<<g, 256, 0, s>>>(L, o);                      \
+        else k_update_fields<QV, ION_FP16C><<<g, 256, 0, s>>>(L, o);                                           \
+    }
+
+}  // namespace ion

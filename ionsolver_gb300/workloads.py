@@ -1,0 +1,101 @@
+"""Synthetic inputs of the benchmark configurations (all seeded, no dataset).
+
+* ``taylor_green``: plain D3Q19 SRT, periodic box, Taylor-Green vortex
+  (u0 = 0.05, rho = 1), tau = 0.6 (nu = 1/30).
+* ``mhd_box``: D3Q19 fluid + D3Q7 charge lattice, one-cell solid shell,
+  charge i.i.d. U[-1e-3, 1e-3] (PCG64 seed 1), velocity N(0, 1e-3^2) per
+  component (seed 2), rho = 1, an axially magnetised disk magnet centred on
+  the z = 1 face, Units{m=1, kg=1, s=1, a=1e-6}, LOD depth 4.
+
+A case is a dict ``{"config": {...C field names...}, "fields": {...},
+"meshes": [(p0, p1, p2, model, values)], "precompute_b": bool}`` that
+``apply_case`` writes into any object with ``write``/``add_mesh``/
+``voxelise_mesh``/``precompute_B`` (the GPU ``Lbm``; tests adapt the CPU
+oracle to the same calls).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .lbm import taylor_green_fields
+from .meshes import annulus, cylinder
+
+NU_1_30 = float(np.float32(1.0) / np.float32(30.0))  # tau = 0.6
+MAGNETIZATION_SI = 8.0e10  # A/m: gives max |B_stat| of a few 1e-2 lattice units with a = 1e-6
+
+
+def taylor_green(n: int = 64, amplitude: float = 0.05, float_type: int = 2, relaxation_time: int = 0,
+                 shape: tuple | None = None) -> dict:
+    nx, ny, nz = shape or (n, n, n)
+    ux, uy, uz, rho = taylor_green_fields(nx, ny, nz, 1, amplitude, reference_density=False)
+    return {
+        "config": dict(velocity_set=2, relaxation_time=relaxation_time, float_type=float_type, n_x=nx, n_y=ny,
+                       n_z=nz, nu=NU_1_30, update_fields=1),
+        "fields": {"u": np.concatenate([ux, uy, uz]), "rho": rho},
+        "meshes": [],
+        "precompute_b": False,
+    }
+
+
+def shell_flags(nx: int, ny: int, nz: int) -> np.ndarray:
+    f = np.zeros((nz, ny, nx), np.uint8)
+    f[0], f[-1] = 1, 1
+    f[:, 0], f[:, -1] = 1, 1
+    f[:, :, 0], f[:, :, -1] = 1, 1
+    return f.reshape(-1)
+
+
+def mhd_box(n: int = 128, float_type: int = 2, depth: int = 4, field_mode: int = 0, magnet_r: float = 16.0,
+            magnet_t: float = 8.0, magnet: bool = True, shape: tuple | None = None, seed_q: int = 1,
+            seed_u: int = 2, update_fields: int = 1, magnetization: float = MAGNETIZATION_SI,
+            rings: bool = False) -> dict:
+    nx, ny, nz = shape or (n, n, n)
+    N = nx * ny * nz
+    q = np.random.Generator(np.random.PCG64(seed_q)).uniform(-1e-3, 1e-3, N).astype(np.float32)
+    u = np.random.Generator(np.random.PCG64(seed_u)).normal(0.0, 1e-3, 3 * N).astype(np.float32)
+    meshes = []
+    if magnet and not rings:
+        p0, p1, p2 = cylinder((0.5 * nx, 0.5 * ny, 1.0 + 0.5 * magnet_t), magnet_r, magnet_t, axis=2)
+        meshes.append((p0, p1, p2, "magnet", (0.0, 0.0, magnetization)))
+    if rings:  # two coaxial ring magnets, R_out 48, R_in 32, t 12, 128 apart (scaled to the box)
+        s = nx / 384.0
+        for zc in (0.5 * nz - 64.0 * s, 0.5 * nz + 64.0 * s):
+            p0, p1, p2 = annulus((0.5 * nx, 0.5 * ny, zc), 48.0 * s, 32.0 * s, 12.0 * s, axis=2)
+            meshes.append((p0, p1, p2, "magnet", (0.0, 0.0, magnetization)))
+    return {
+        "config": dict(velocity_set=2, relaxation_time=0, float_type=float_type, n_x=nx, n_y=ny, n_z=nz,
+                       nu=NU_1_30, ext_volume_force=1, ext_magneto_hydro=1, mhd_lod_depth=depth,
+                       update_fields=update_fields, field_mode=field_mode,
+                       units=dict(m=1.0, kg=1.0, s=1.0, a=1e-6, k=1.0, prop=0)),
+        "fields": {"flags": shell_flags(nx, ny, nz), "q": q, "u": u, "rho": np.ones(N, np.float32)},
+        "meshes": meshes,
+        "precompute_b": bool(meshes),
+    }
+
+
+MODEL_IDS = {"solid": 0, "magnet": 1, "charged": 2, "charged_ecr": 3}
+
+
+def lbm_config(case: dict):
+    """The case's config as an LbmConfig."""
+    from .lbm import LbmConfig, Units
+    c = dict(case["config"])
+    units = c.pop("units", None)
+    if "ext_equilibrium_boundaries" in c:
+        c["ext_equilibrium_boudaries"] = c.pop("ext_equilibrium_boundaries")
+    cfg = LbmConfig(**c)
+    if units:
+        cfg.units = Units(**units)
+    return cfg
+
+
+def apply_case(lbm, case: dict) -> None:
+    """Writes the case's fields and magnets into a GPU Lbm (order: fields, voxelise, precompute_B)."""
+    from .lbm import ModelType
+    for name, arr in case["fields"].items():
+        lbm.write(name, arr)
+    for p0, p1, p2, model, vals in case["meshes"]:
+        idx = lbm.add_mesh(p0, p1, p2)
+        lbm.voxelise_mesh(idx, ModelType(MODEL_IDS[model], tuple(vals)))
+    if case["precompute_b"]:
+        lbm.precompute_B()

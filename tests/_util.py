@@ -1,0 +1,84 @@
+"""Shared helpers of the test-suite: run one synthetic case on the GPU and on
+a CPU oracle, and compare the results."""
+from __future__ import annotations
+
+import numpy as np
+
+import oracle as O
+from ionsolver_gb300 import workloads as W
+
+MODEL_NAMES = {v: k for k, v in W.MODEL_IDS.items()}
+
+
+def oracle_config(case):
+    return O.make_config(**case["config"])
+
+
+def setup_oracle(case, kind="f32", threads=None):
+    o = O.OracleLbm(oracle_config(case), kind, threads or O.cpu_count())
+    for name, arr in case["fields"].items():
+        o.set_field(name, arr)
+    for p0, p1, p2, model, vals in case["meshes"]:
+        o.voxelise(p0, p1, p2, model, vals)
+    if case["precompute_b"]:
+        o.precompute_b()
+    return o
+
+
+def run_oracle(case, steps, kind="f32", threads=None):
+    o = setup_oracle(case, kind, threads)
+    o.initialize()
+    o.run(steps)
+    return o
+
+
+def setup_gpu(case):
+    import ionsolver_gb300 as I
+    lbm = I.Lbm(W.lbm_config(case))
+    W.apply_case(lbm, case)
+    return lbm
+
+
+def run_gpu(case, steps, graph=True):
+    lbm = setup_gpu(case)
+    lbm.initialize()
+    if graph:
+        lbm.run(steps)
+    else:
+        for _ in range(steps):
+            lbm.do_time_step()
+    lbm.finish_queues(120000)
+    return lbm
+
+
+def field_names(case):
+    names = ["fi", "rho", "u", "flags"]
+    if case["config"].get("ext_magneto_hydro"):
+        names += ["fqi", "ei", "q", "e_dyn", "b_dyn", "b_stat", "e_stat", "qu_lod"]
+    return names
+
+
+def bit_diff(a: np.ndarray, b: np.ndarray) -> int:
+    """Number of elements whose bit patterns differ."""
+    assert a.dtype.itemsize == b.dtype.itemsize and a.size == b.size, (a.dtype, b.dtype, a.size, b.size)
+    ia = a.view(np.uint8).reshape(a.size, a.dtype.itemsize)
+    ib = b.view(np.uint8).reshape(b.size, b.dtype.itemsize)
+    return int(np.any(ia != ib, axis=1).sum())
+
+
+def compare_bitwise(gpu, orc, names):
+    out = {}
+    for n in names:
+        g = gpu.read(n)
+        o = orc.field(n)
+        out[n] = bit_diff(g, o.astype(g.dtype) if o.dtype != g.dtype else o)
+    return out
+
+
+def rel_err(a, b):
+    """max |a-b| / max |b| (normwise relative error)."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    d = np.max(np.abs(a - b)) if a.size else 0.0
+    s = np.max(np.abs(b)) if b.size else 0.0
+    return float(d / s) if s > 0 else float(d)

@@ -1,0 +1,148 @@
+"""GPU kernels against the CPU oracle on the same seeded inputs.
+
+Bar: bit-identical results (integer and floating point) for the timestep in
+BITWISE field mode, the voxeliser and the static magnet field; the FAST
+field mode within a stated relative error."""
+import numpy as np
+import pytest
+
+import oracle as O
+from ionsolver_gb300 import workloads as W
+from tests import _util as U
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("ft", [2, 0, 1], ids=["FP32", "FP16S", "FP16C"])
+@pytest.mark.parametrize("rt", [0, 1], ids=["SRT", "TRT"])
+def test_plain_taylor_green_bitwise(ft, rt):
+    case = W.taylor_green(shape=(32, 24, 16), amplitude=0.05, float_type=ft, relaxation_time=rt)
+    g = U.run_gpu(case, 100)
+    o = U.run_oracle(case, 100)
+    assert U.compare_bitwise(g, o, ["fi", "rho", "u"]) == {"fi": 0, "rho": 0, "u": 0}
+
+
+@pytest.mark.parametrize("vs,shape", [(1, (16, 12, 10)), (0, (40, 24, 1))], ids=["D3Q15", "D2Q9"])
+def test_other_velocity_sets_bitwise(vs, shape):
+    case = W.taylor_green(shape=shape, amplitude=0.05)
+    case["config"]["velocity_set"] = vs
+    if vs == 0:  # a 2-D shear field (the 3-D vortex has no in-plane flow at n_z = 1)
+        n2 = shape[0] * shape[1]
+        rng = np.random.default_rng(11)
+        case["fields"]["u"] = np.concatenate([rng.normal(0, 0.02, 2 * n2), np.zeros(n2)]).astype(np.float32)
+    g = U.run_gpu(case, 50)
+    o = U.run_oracle(case, 50)
+    assert U.compare_bitwise(g, o, ["fi", "rho", "u"]) == {"fi": 0, "rho": 0, "u": 0}
+
+
+@pytest.mark.parametrize("rt", [0, 1], ids=["SRT", "TRT"])
+def test_boundaries_and_forces_bitwise(rt):
+    """Solid cells, equilibrium (inflow/outflow) cells, volume force and force field."""
+    nx, ny, nz = 24, 20, 16
+    N = nx * ny * nz
+    rng = np.random.default_rng(7)
+    case = W.taylor_green(shape=(nx, ny, nz), amplitude=0.03, relaxation_time=rt)
+    flags = W.shell_flags(nx, ny, nz)
+    flags.reshape(nz, ny, nx)[:, :, 0] = 0x02      # equilibrium inlet plane
+    flags.reshape(nz, ny, nx)[4:8, 5:9, 6:10] = 0x01  # an obstacle
+    case["fields"]["flags"] = flags
+    case["fields"]["F"] = rng.normal(0, 1e-5, 3 * N).astype(np.float32)
+    case["fields"]["rho"] = (1.0 + rng.normal(0, 1e-3, N)).astype(np.float32)
+    case["config"].update(ext_equilibrium_boundaries=1, ext_volume_force=1, ext_force_field=1,
+                          f_x=1e-6, f_y=-2e-6, f_z=5e-7)
+    g = U.run_gpu(case, 60)
+    o = U.run_oracle(case, 60)
+    assert U.compare_bitwise(g, o, ["fi", "rho", "u", "flags"]) == {"fi": 0, "rho": 0, "u": 0, "flags": 0}
+
+
+@pytest.mark.parametrize("ft", [2, 0, 1], ids=["FP32", "FP16S", "FP16C"])
+@pytest.mark.parametrize("n,depth,r,t", [(32, 4, 6.0, 4.0), (16, 2, 4.0, 3.0), (24, 3, 5.0, 4.0)],
+                         ids=["32c-D4", "16c-D2", "24c-D3"])
+def test_mhd_bitwise(ft, n, depth, r, t):
+    case = W.mhd_box(n=n, float_type=ft, depth=depth, magnet_r=r, magnet_t=t, field_mode=0)
+    g = U.run_gpu(case, 12)
+    o = U.run_oracle(case, 12)
+    diff = U.compare_bitwise(g, o, U.field_names(case))
+    assert all(v == 0 for v in diff.values()), diff
+
+
+def test_mhd_fast_field_close():
+    """FAST field mode: same sources and order, rsqrt/FMA arithmetic."""
+    case = W.mhd_box(n=32, depth=4, magnet_r=6.0, magnet_t=4.0, field_mode=1)
+    g = U.run_gpu(case, 1)
+    ref_case = dict(case, config=dict(case["config"], field_mode=0))
+    o = U.run_oracle(ref_case, 1)
+    # dynamic part of the field only: subtract the static field first
+    for dyn, stat in (("e_dyn", "e_stat"), ("b_dyn", "b_stat")):
+        N = 32 ** 3
+        gd = g.read(dyn)[:3 * N].astype(np.float64) - g.read(stat).astype(np.float64)
+        od = o.field(dyn)[:3 * N].astype(np.float64) - o.field(stat).astype(np.float64)
+        assert U.rel_err(gd, od) < 1e-4, dyn
+
+
+def test_voxelise_and_static_field_bitwise():
+    case = W.mhd_box(n=32, depth=4, magnet_r=7.0, magnet_t=5.0)
+    case["meshes"].append(tuple(list(W.annulus((16.0, 16.0, 22.0), 9.0, 5.0, 3.0, axis=0)) + ["solid", (0, 0, 0)]))
+    g = U.setup_gpu(case)
+    o = U.setup_oracle(case)
+    d = U.compare_bitwise(g, o, ["flags", "b_dyn", "b_stat", "e_dyn"])
+    assert d == {"flags": 0, "b_dyn": 0, "b_stat": 0, "e_dyn": 0}
+    flags = g.read("flags")
+    assert (flags == 0x11).sum() > 100 and ((flags & 0x1F) == 0x01).sum() > 0
+
+
+def test_static_e_bitwise():
+    case = W.mhd_box(n=16, depth=2, magnet=False)
+    p = W.cylinder((8.0, 8.0, 8.0), 3.0, 3.0, axis=1)
+    case["meshes"] = [(p[0], p[1], p[2], "charged", (2e-9, 0, 0))]
+    g = U.setup_gpu(case)
+    g.precompute_E()
+    o = U.setup_oracle(case)
+    o.precompute_e()
+    assert U.compare_bitwise(g, o, ["flags", "e_stat", "b_dyn"]) == {"flags": 0, "e_stat": 0, "b_dyn": 0}
+
+
+def test_update_fields_bitwise():
+    case = W.taylor_green(shape=(16, 16, 16))
+    case["config"]["update_fields"] = 0
+    g = U.run_gpu(case, 7)
+    o = U.run_oracle(case, 7)
+    g.update_fields()
+    o.update_fields()
+    assert U.compare_bitwise(g, o, ["rho", "u"]) == {"rho": 0, "u": 0}
+
+
+def test_graph_run_equals_single_steps():
+    case = W.mhd_box(n=16, depth=2, magnet_r=4.0, magnet_t=3.0)
+    a = U.run_gpu(case, 37, graph=True)
+    b = U.run_gpu(case, 37, graph=False)
+    assert a.get_time_step() == b.get_time_step() == 37
+    for name in U.field_names(case):
+        assert U.bit_diff(a.read(name), b.read(name)) == 0, name
+
+
+def test_mass_and_charge_conservation_fp64():
+    case = W.mhd_box(n=32, depth=4, magnet_r=6.0, magnet_t=4.0, field_mode=1)
+    g = U.setup_gpu(case)
+    g.initialize()
+    m0, q0 = g.mass_charge()
+    g.run(200)
+    m1, q1 = g.mass_charge()
+    assert abs(m1 - m0) / m0 < 1e-6
+    assert abs(q1 - q0) < 1e-6 * max(1.0, abs(q0))
+
+
+def test_codecs_exhaustive_against_oracle():
+    import ionsolver_gb300 as I
+    lib = O.oracle_lib("f32")
+    raw = np.arange(65536, dtype=np.uint16)
+    rng = np.random.default_rng(3)
+    vals = np.concatenate([rng.uniform(-2.0, 2.0, 40000), rng.normal(0, 1e-3, 20000),
+                           np.ldexp(rng.uniform(-1, 1, 5536), rng.integers(-30, 2, 5536))]).astype(np.float32)
+    for ft, enc_f, dec_f in ((0, lib.orc_fp16s_encode, lib.orc_fp16s_decode), (1, lib.orc_fp16c_encode, lib.orc_fp16c_decode)):
+        enc, dec, rdec = I.codec_roundtrip(ft, vals, raw)
+        e_ref = np.array([enc_f(float(v)) for v in vals], np.uint16)
+        d_ref = np.array([dec_f(int(r)) for r in raw], np.float32)
+        assert np.array_equal(enc, e_ref)
+        finite = np.isfinite(d_ref)
+        assert np.array_equal(rdec[finite].view(np.uint32), d_ref[finite].view(np.uint32))
