@@ -105,8 +105,14 @@ __host__ __device__ __forceinline__ float bitsf(uint32_t u) {
 #endif
 }
 
+// A NaN is encoded as the canonical quiet NaN 0x7FFFFFFF would be (the bit
+// pattern NVIDIA hardware gives every NaN result), so the stored value does
+// not depend on where a NaN came from.  The reference's MHD step produces
+// NaNs by itself: its electron density starts at 0 (sim_kernels.cl:823) and
+// reaches exactly 0 again, so u_e = 0/0 (sim_kernels.cl:230-232).
 __host__ __device__ __forceinline__ uint16_t fp16c_encode(float x) {
-    const uint32_t b = fbits(x) + 0x800u;
+    const uint32_t xb = fbits(x);
+    const uint32_t b = (((xb & 0x7FFFFFFFu) > 0x7F800000u) ? 0x7FFFFFFFu : xb) + 0x800u;
     const uint32_t e = (b & 0x7F800000u) >> 23, m = b & 0x007FFFFFu;
     uint32_t out = (b & 0x80000000u) >> 16;
     if (e > 112u) out |= (((e - 112u) << 11) & 0x7800u) | (m >> 12);

@@ -145,10 +145,114 @@ struct Nb7 {  // D3Q7 subset (sim_kernels.cl:382-389)
 };
 
 // ---------------------------------------------------------------------------
+// Fused equilibrium / forcing / collision / store, one direction pair at a
+// time.  Each value is computed with exactly the operations of
+// equilibrium() / forcing() above and of the reference's collision loops
+// (sim_kernels.cl:714-754); only the order in which independent directions
+// are finished changes, which keeps far fewer values live in registers.
+// ---------------------------------------------------------------------------
+struct EqState {
+    float rho, rm1, c3, ux, uy, uz;  // u already multiplied by 3
+};
+__device__ __forceinline__ EqState eq_state(float rho, float ux, float uy, float uz) {
+    EqState s;
+    s.c3 = -3.0f * ((ux * ux + uy * uy) + uz * uz);
+    s.rm1 = rho - 1.0f;
+    s.rho = rho;
+    s.ux = ux * 3.0f; s.uy = uy * 3.0f; s.uz = uz * 3.0f;
+    return s;
+}
+template <class V>
+__device__ __forceinline__ float eq_zero(const EqState& s) { return V::w(0) * fmaf(s.rho, 0.5f * s.c3, s.rm1); }
+template <class V>
+__device__ __forceinline__ void eq_pair(const EqState& s, int i, float& a, float& b) {
+    const float wr = V::w(V::wc(i)) * s.rho, wrm1 = V::w(V::wc(i)) * s.rm1;
+    const float p = project<V>(i, s.ux, s.uy, s.uz);
+    a = fmaf(wr, fmaf(0.5f, fmaf(p, p, s.c3), p), wrm1);
+    b = fmaf(wr, fmaf(0.5f, fmaf(p, p, s.c3), -p), wrm1);
+}
+struct ForceState {
+    float ux, uy, uz, fx, fy, fz, uF;
+};
+template <class V>
+__device__ __forceinline__ ForceState force_state(float ux, float uy, float uz, float fx, float fy, float fz) {
+    ForceState s{ux, uy, uz, fx, fy, fz, 0.0f};
+    s.uF = V::dims == 2 ? -THIRD * fmaf(ux, fx, uy * fy) : -THIRD * fmaf(ux, fx, fmaf(uy, fy, uz * fz));
+    return s;
+}
+template <class V>
+__device__ __forceinline__ float force_dir(const ForceState& s, int i) {
+    if (i == 0) return (9.0f * V::w(0)) * s.uF;
+    const float cx = (float)V::c(i, 0), cy = (float)V::c(i, 1), cz = (float)V::c(i, 2);
+    const float cf = (cx * s.fx + cy * s.fy) + cz * s.fz;
+    const float cu = ((cx * s.ux + cy * s.uy) + cz * s.uz) + THIRD;
+    return (9.0f * V::w(V::wc(i))) * fmaf(cf, cu, s.uF);
+}
+
+// SRT collision + Esoteric-Pull store (sim_kernels.cl:714-723 / 649-656).
+// force: 0 = none (Fin = 0), 1 = Guo terms scaled by c_tau.
+template <class V, class D, class NB>
+__device__ __forceinline__ void srt_store(typename D::T* f, uint32_t N, uint32_t n, bool odd, const NB& j, const float* fh,
+                                          const EqState& es, const ForceState& fs, bool force, float c_tau, float w,
+                                          bool eqc) {
+    {
+        const float feq = eq_zero<V>(es);
+        const float F = force ? force_dir<V>(fs, 0) * c_tau : 0.0f;
+        D::st(f, n, eqc ? feq : fmaf(1.0f - w, fh[0], fmaf(w, feq, F)));
+    }
+#pragma unroll
+    for (int i = 1; i < V::q; i += 2) {
+        float fa, fb;
+        eq_pair<V>(es, i, fa, fb);
+        const float Fa = force ? force_dir<V>(fs, i) * c_tau : 0.0f;
+        const float Fb = force ? force_dir<V>(fs, i + 1) * c_tau : 0.0f;
+        const float va = eqc ? fa : fmaf(1.0f - w, fh[i], fmaf(w, fa, Fa));
+        const float vb = eqc ? fb : fmaf(1.0f - w, fh[i + 1], fmaf(w, fb, Fb));
+        D::st(f, (size_t)(odd ? i + 1 : i) * N + j(i), va);
+        D::st(f, (size_t)(odd ? i : i + 1) * N + n, vb);
+    }
+}
+
+// TRT collision + store (sim_kernels.cl:725-754)
+template <class V, class D, class NB>
+__device__ __forceinline__ void trt_store(typename D::T* f, uint32_t N, uint32_t n, bool odd, const NB& j, const float* fh,
+                                          const EqState& es, const ForceState& fs, bool force, float w, bool eqc) {
+    const float wp = w, wm = 1.0f / (0.1875f / (1.0f / w - 0.5f) + 0.5f);
+    const float ctp = fmaf(wp, -0.25f, 0.5f), ctm = fmaf(wm, -0.25f, 0.5f);
+    {
+        const float feq = eq_zero<V>(es);
+        float F = 0.0f;
+        if (force) {
+            const float F0 = force_dir<V>(fs, 0);
+            F = fmaf(ctp, F0 + F0, ctm * (F0 - F0));
+        }
+        const float sym = ((feq - fh[0]) + feq) - fh[0];
+        const float asym = ((feq - feq) - fh[0]) + fh[0];
+        D::st(f, n, eqc ? feq : fmaf(0.5f * wp, sym, fmaf(0.5f * wm, asym, fh[0] + F)));
+    }
+#pragma unroll
+    for (int i = 1; i < V::q; i += 2) {
+        float ea, eb;
+        eq_pair<V>(es, i, ea, eb);
+        float Fa = 0.0f, Fb = 0.0f;
+        if (force) {
+            const float A = force_dir<V>(fs, i), B = force_dir<V>(fs, i + 1);
+            Fa = fmaf(ctp, A + B, ctm * (A - B));
+            Fb = fmaf(ctp, B + A, ctm * (B - A));
+        }
+        const float ha = fh[i], hb = fh[i + 1];
+        const float va = eqc ? ea : fmaf(0.5f * wp, ((ea - ha) + eb) - hb, fmaf(0.5f * wm, ((ea - eb) - ha) + hb, ha + Fa));
+        const float vb = eqc ? eb : fmaf(0.5f * wp, ((eb - hb) + ea) - ha, fmaf(0.5f * wm, ((eb - ea) - hb) + ha, hb + Fb));
+        D::st(f, (size_t)(odd ? i + 1 : i) * N + j(i), va);
+        D::st(f, (size_t)(odd ? i : i + 1) * N + n, vb);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // stream_collide, one step (sim_kernels.cl:465-758)
 // ---------------------------------------------------------------------------
 template <int Q, int FT, bool MHD, bool TRT>
-__global__ void __launch_bounds__(256) k_stream_collide(const DevLbm L, const uint32_t odd_t) {
+__global__ void __launch_bounds__(256, MHD ? 2 : 3) k_stream_collide(const DevLbm L, const uint32_t odd_t) {
     using V = VSet<Q>;
     using D = Ddf<FT>;
     using T = typename D::T;
@@ -162,7 +266,7 @@ __global__ void __launch_bounds__(256) k_stream_collide(const DevLbm L, const ui
         cell_xyz(L, n, x, y, z);
         const Nbr nb(L, x, y, z);
         const NbV<V> j{nb};
-        float fhn[Q], feq[Q], Fin[Q];
+        float fhn[Q];
         ep_load<D, Q>((const T*)L.fi, N, n, odd, j, fhn);
         float rhon, uxn, uyn, uzn;
         if (eqc) { rhon = L.rho[n]; uxn = L.u[n]; uyn = L.u[(size_t)N + n]; uzn = L.u[2 * (size_t)N + n]; }
@@ -176,45 +280,46 @@ __global__ void __launch_bounds__(256) k_stream_collide(const DevLbm L, const ui
         if constexpr (MHD) {
             const float Bx = L.b_dyn[n], By = L.b_dyn[(size_t)N + n], Bz = L.b_dyn[2 * (size_t)N + n];
             const float Ex = L.e_dyn[n], Ey = L.e_dyn[(size_t)N + n], Ez = L.e_dyn[2 * (size_t)N + n];
-            // electron gas, part 1
-            float ehn[Q];
-            ep_load<D, Q>((const T*)L.ei, N, n, odd, j, ehn);
-            float rhoe, uxe, uye, uze;
-            moments<V>(ehn, rhoe, uxe, uye, uze);
-            // charge advection (D3Q7)
+            // charge advection (D3Q7): load, charge, collide, store
             const Nb7 j7{nb};
-            float qhn[7];
-            ep_load<D, 7>((const T*)L.fqi, N, n, odd, j7, qhn);
-            float rhoq = 0.0f;
+            float rhoq;
+            {
+                float qhn[7];
+                ep_load<D, 7>((const T*)L.fqi, N, n, odd, j7, qhn);
+                rhoq = 0.0f;
 #pragma unroll
-            for (int i = 0; i < 7; i++) rhoq = rhoq + qhn[i];
-            rhoq = rhoq + 1.0f;
+                for (int i = 0; i < 7; i++) rhoq = rhoq + qhn[i];
+                rhoq = rhoq + 1.0f;
+                float aeq[7];
+                adv_equilibrium(rhoq, uxn, uyn, uzn, aeq);
+#pragma unroll
+                for (int i = 0; i < 7; i++) qhn[i] = fmaf(1.0f - L.wq, qhn[i], L.wq * aeq[i]);
+                ep_store<D, 7>((T*)L.fqi, N, n, odd, j7, qhn);
+            }
+            // electron gas: moments, Lorentz force, Guo half-step, SRT, store
+            float rhoe;
+            {
+                float ehn[Q];
+                ep_load<D, Q>((const T*)L.ei, N, n, odd, j, ehn);
+                float uxe, uye, uze;
+                moments<V>(ehn, rhoe, uxe, uye, uze);
+                const float cxv = uye * Bz - uze * By, cyv = uze * Bx - uxe * Bz, czv = uxe * By - uye * Bx;
+                const float nre = -rhoe;
+                const float efx = nre * (Ex + cxv), efy = nre * (Ey + cyv), efz = nre * (Ez + czv);
+                const float r2e = 0.5f / (rhoe * L.kkge);
+                uxe = clampf(fmaf(efx, r2e, uxe), -CS, CS);
+                uye = clampf(fmaf(efy, r2e, uye), -CS, CS);
+                uze = clampf(fmaf(efz, r2e, uze), -CS, CS);
+                const ForceState fe = force_state<V>(uxe, uye, uze, efx, efy, efz);
+                const EqState ee = eq_state(rhoe, uxe, uye, uze);
+                srt_store<V, D>((T*)L.ei, N, n, odd, j, ehn, ee, fe, true, c_tau, w, eqc);
+            }
             L.q[n] = rhoq - rhoe;
-            float aeq[7];
-            adv_equilibrium(rhoq, uxn, uyn, uzn, aeq);
-#pragma unroll
-            for (int i = 0; i < 7; i++) qhn[i] = fmaf(1.0f - L.wq, qhn[i], L.wq * aeq[i]);
-            ep_store<D, 7>((T*)L.fqi, N, n, odd, j7, qhn);
-            // electron gas, part 2: Lorentz force, Guo half-step, SRT
-            const float cxv = uye * Bz - uze * By, cyv = uze * Bx - uxe * Bz, czv = uxe * By - uye * Bx;
-            const float nre = -rhoe;
-            const float efx = nre * (Ex + cxv), efy = nre * (Ey + cyv), efz = nre * (Ez + czv);
-            const float r2e = 0.5f / (rhoe * L.kkge);
-            uxe = clampf(fmaf(efx, r2e, uxe), -CS, CS);
-            uye = clampf(fmaf(efy, r2e, uye), -CS, CS);
-            uze = clampf(fmaf(efz, r2e, uze), -CS, CS);
-            forcing<V>(uxe, uye, uze, efx, efy, efz, Fin);
-            equilibrium<V>(rhoe, uxe, uye, uze, feq);
-#pragma unroll
-            for (int i = 0; i < Q; i++) Fin[i] = Fin[i] * c_tau;
-#pragma unroll
-            for (int i = 0; i < Q; i++) ehn[i] = eqc ? feq[i] : fmaf(1.0f - w, ehn[i], fmaf(w, feq[i], Fin[i]));
-            ep_store<D, Q>((T*)L.ei, N, n, odd, j, ehn);
             // Lorentz force on the gas
             fxn = fxn + rhoq * ((Ex + uyn * Bz) - uzn * By);
             fyn = fyn + rhoq * ((Ey + uzn * Bx) - uxn * Bz);
             fzn = fzn + rhoq * ((Ez + uxn * By) - uyn * Bx);
-            // LOD contribution: velocity / bin volume (charge is q[n])
+            // LOD contribution: velocity / bin volume (the charge is q[n])
             if (L.depth > 0u) {
                 L.lod_cell[n] = uxn * L.ils;
                 L.lod_cell[(size_t)N + n] = uyn * L.ils;
@@ -227,49 +332,19 @@ __global__ void __launch_bounds__(256) k_stream_collide(const DevLbm L, const ui
             uxn = clampf(fmaf(fxn, r2, uxn), -CS, CS);
             uyn = clampf(fmaf(fyn, r2, uyn), -CS, CS);
             uzn = clampf(fmaf(fzn, r2, uzn), -CS, CS);
-            forcing<V>(uxn, uyn, uzn, fxn, fyn, fzn, Fin);
         } else {
             uxn = clampf(uxn, -CS, CS);
             uyn = clampf(uyn, -CS, CS);
             uzn = clampf(uzn, -CS, CS);
-#pragma unroll
-            for (int i = 0; i < Q; i++) Fin[i] = 0.0f;
         }
         if (L.update_fields && !eqc) {
             L.rho[n] = rhon;
             L.u[n] = uxn; L.u[(size_t)N + n] = uyn; L.u[2 * (size_t)N + n] = uzn;
         }
-        equilibrium<V>(rhon, uxn, uyn, uzn, feq);
-        if constexpr (TRT) {
-            const float wp = w, wm = 1.0f / (0.1875f / (1.0f / w - 0.5f) + 0.5f);
-            if (L.ext_vf) {
-                const float ctp = fmaf(wp, -0.25f, 0.5f), ctm = fmaf(wm, -0.25f, 0.5f);
-                float Fb[Q];
-                Fb[0] = Fin[0];
-#pragma unroll
-                for (int i = 1; i < Q; i += 2) { Fb[i] = Fin[i + 1]; Fb[i + 1] = Fin[i]; }
-#pragma unroll
-                for (int i = 0; i < Q; i++) Fin[i] = fmaf(ctp, Fin[i] + Fb[i], ctm * (Fin[i] - Fb[i]));
-            }
-            float fb[Q], eb[Q];
-            fb[0] = fhn[0]; eb[0] = feq[0];
-#pragma unroll
-            for (int i = 1; i < Q; i += 2) { fb[i] = fhn[i + 1]; fb[i + 1] = fhn[i]; eb[i] = feq[i + 1]; eb[i + 1] = feq[i]; }
-#pragma unroll
-            for (int i = 0; i < Q; i++) {
-                const float sym = ((feq[i] - fhn[i]) + eb[i]) - fb[i];
-                const float asym = ((feq[i] - eb[i]) - fhn[i]) + fb[i];
-                fhn[i] = eqc ? feq[i] : fmaf(0.5f * wp, sym, fmaf(0.5f * wm, asym, fhn[i] + Fin[i]));
-            }
-        } else {
-            if (L.ext_vf) {
-#pragma unroll
-                for (int i = 0; i < Q; i++) Fin[i] = Fin[i] * c_tau;
-            }
-#pragma unroll
-            for (int i = 0; i < Q; i++) fhn[i] = eqc ? feq[i] : fmaf(1.0f - w, fhn[i], fmaf(w, feq[i], Fin[i]));
-        }
-        ep_store<D, Q>((T*)L.fi, N, n, odd, j, fhn);
+        const EqState es = eq_state(rhon, uxn, uyn, uzn);
+        const ForceState fs = force_state<V>(uxn, uyn, uzn, fxn, fyn, fzn);
+        if constexpr (TRT) trt_store<V, D>((T*)L.fi, N, n, odd, j, fhn, es, fs, L.ext_vf, w, eqc);
+        else srt_store<V, D>((T*)L.fi, N, n, odd, j, fhn, es, fs, L.ext_vf, c_tau, w, eqc);
     }
 }
 

@@ -103,6 +103,8 @@ def _bind(lib: C.CDLL) -> C.CDLL:
     lib.orc_time_step.restype = C.c_uint64
     lib.orc_time_step.argtypes = [C.c_void_p]
     lib.orc_set_threads.argtypes = [C.c_int]
+    if hasattr(lib, "orc_set_nan_model"):
+        lib.orc_set_nan_model.argtypes = [C.c_int]
     fp = C.POINTER(C.c_float)
     lib.orc_voxelize.restype = C.c_int
     lib.orc_voxelize.argtypes = [C.c_void_p, fp, fp, fp, C.c_uint32, fp, fp, C.c_int, C.c_float, C.c_float,
@@ -156,7 +158,7 @@ def constants(cfg: IonConfig) -> IonConstants:
 class OracleLbm:
     """One domain advanced by a CPU oracle; mirrors the product's Lbm class."""
 
-    def __init__(self, cfg: IonConfig, kind: str = "f32", threads: int = 1):
+    def __init__(self, cfg: IonConfig, kind: str = "f32", threads: int = 1, canonical_nan: bool = False):
         self.cfg = cfg
         self.kind = kind
         if kind == "ref":
@@ -167,6 +169,7 @@ class OracleLbm:
             lib = oracle_lib(kind)
         self.lib = lib
         self.threads = threads
+        self.canonical_nan = canonical_nan
         k = constants(cfg)
         h = lib.orc_create(C.byref(cfg), C.byref(k))
         if not h:
@@ -186,6 +189,8 @@ class OracleLbm:
 
     def _threads(self):
         self.lib.orc_set_threads(int(self.threads))
+        if hasattr(self.lib, "orc_set_nan_model"):
+            self.lib.orc_set_nan_model(int(self.canonical_nan))
 
     @property
     def n(self) -> int:

@@ -112,8 +112,15 @@ static uint16_t ieee_float_to_half_rne(float f) {
 /* FP16C encode: round by adding 2^11 to the float's bit pattern, then keep
  * 4 exponent bits (bias 15) and 11 mantissa bits; small magnitudes become
  * 1-4-11 denormals, anything below goes to signed zero. */
+/* NaN model: 0 = the host's NaN bit patterns (as the reference kernels
+ * compiled for this host produce them); 1 = every NaN reaching the FP16C
+ * encoder is the canonical quiet NaN 0x7FFFFFFF, the pattern NVIDIA GPUs
+ * give NaN results (the GPU implementation's rule). */
+static int g_canonical_nan = 0;
+void orc_set_nan_model(int canonical) { g_canonical_nan = canonical != 0; }
 static uint16_t fp16c_encode(float x) {
-    const uint32_t b = f2u(x) + 0x800u;
+    const uint32_t xb = f2u(x);
+    const uint32_t b = ((g_canonical_nan && (xb & 0x7FFFFFFFu) > 0x7F800000u) ? 0x7FFFFFFFu : xb) + 0x800u;
     const uint32_t e = (b & 0x7F800000u) >> 23, m = b & 0x007FFFFFu;
     uint32_t out = (b & 0x80000000u) >> 16;
     if (e > 112u) out |= (((e - 112u) << 11) & 0x7800u) | (m >> 12);

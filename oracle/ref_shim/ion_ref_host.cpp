@@ -315,4 +315,11 @@ void orc_precompute_e(void* p) {
 
 int orc_kind(void) { return 1; }  // 1 = the reference's kernels
 
+// the reference's FP16C codec functions (sim_kernels.cl:79-90) and the
+// FP16S load/store macros of get_device_defines (domain.rs:773-776)
+uint16_t orc_fp16c_encode(float x) { return float_to_half_custom(x); }
+float orc_fp16c_decode(uint16_t x) { return half_to_float_custom(x); }
+uint16_t orc_fp16s_encode(float x) { half h[1]; vstore_half_rte((x) * 32768.0f, 0, h); return h[0]; }
+float orc_fp16s_decode(uint16_t x) { const half h[1] = {x}; return vload_half(0, h) * 3.0517578E-5f; }
+
 }  // extern "C"

@@ -14,8 +14,9 @@ def oracle_config(case):
     return O.make_config(**case["config"])
 
 
-def setup_oracle(case, kind="f32", threads=None):
-    o = O.OracleLbm(oracle_config(case), kind, threads or O.cpu_count())
+def setup_oracle(case, kind="f32", threads=None, canonical_nan=False):
+    o = O.OracleLbm(oracle_config(case), kind, threads or O.cpu_count(), canonical_nan)
+    o._threads()
     for name, arr in case["fields"].items():
         o.set_field(name, arr)
     for p0, p1, p2, model, vals in case["meshes"]:
@@ -25,8 +26,8 @@ def setup_oracle(case, kind="f32", threads=None):
     return o
 
 
-def run_oracle(case, steps, kind="f32", threads=None):
-    o = setup_oracle(case, kind, threads)
+def run_oracle(case, steps, kind="f32", threads=None, canonical_nan=False):
+    o = setup_oracle(case, kind, threads, canonical_nan)
     o.initialize()
     o.run(steps)
     return o
@@ -66,12 +67,35 @@ def bit_diff(a: np.ndarray, b: np.ndarray) -> int:
     return int(np.any(ia != ib, axis=1).sum())
 
 
+def _nan_mask(a: np.ndarray, float_type: int | None) -> np.ndarray:
+    if a.dtype == np.float32 or a.dtype == np.float64:
+        return np.isnan(a)
+    if a.dtype == np.uint16 and float_type == 0:  # FP16S: IEEE half NaN
+        return ((a & 0x7C00) == 0x7C00) & ((a & 0x03FF) != 0)
+    return np.zeros(a.shape, bool)
+
+
+def bit_diff_nan(a: np.ndarray, b: np.ndarray, float_type: int | None = None) -> int:
+    """Elements whose bits differ, counting two NaNs as equal (IEEE leaves NaN
+    payloads to the hardware: GPUs return one canonical NaN, CPUs propagate
+    operand payloads)."""
+    na, nb = _nan_mask(a, float_type), _nan_mask(b, float_type)
+    both = na & nb
+    ia = a.view(np.uint8).reshape(a.size, a.dtype.itemsize)
+    ib = b.view(np.uint8).reshape(b.size, b.dtype.itemsize)
+    return int((np.any(ia != ib, axis=1) & ~both).sum())
+
+
 def compare_bitwise(gpu, orc, names):
+    """Bit-level comparison of GPU and oracle fields (NaN equals NaN)."""
+    ft = int(orc.cfg.float_type)
     out = {}
     for n in names:
         g = gpu.read(n)
         o = orc.field(n)
-        out[n] = bit_diff(g, o.astype(g.dtype) if o.dtype != g.dtype else o)
+        if o.dtype != g.dtype:
+            o = o.astype(g.dtype)
+        out[n] = bit_diff_nan(g, o, ft if n in ("fi", "fqi", "ei") else None)
     return out
 
 
