@@ -1,32 +1,41 @@
 #!/usr/bin/env python3
 """Benchmark of the IonSolver MHD-LBM timestep on GB300 (one JSON line on rank 0).
 
-Workload (default ``mhd128``): 128^3 D3Q19 fluid + D3Q7 charge lattice,
-FP32 storage, tau = 0.6, one-cell solid walls, charge U[-1e-3,1e-3] (seed 1),
-velocity N(0,1e-3^2) (seed 2), an axially magnetised disk magnet (r 16,
-t 8) on the z=1 face, exact LOD E/B update every step (LOD depth 4).  A
-"step" is one timestep of the whole domain: stream_collide, LOD bin sums,
-E/B update.  Metric: MLUPs/s = cells * steps / seconds / 1e6.
+Workloads (``--workload``; default ``mhd128``, the headline configuration):
+  mhd128 / mhd256 : D3Q19 fluid + D3Q7 charge lattice + electron gas, FP32
+      storage (``--float-type`` for FP16S/FP16C), tau 0.6, one-cell solid walls,
+      charge U[-1e-3,1e-3] (seed 1), velocity N(0,1e-3^2) (seed 2), an axially
+      magnetised disk magnet (r 16, t 8 at 128^3) on the z = 1 face, LOD depth
+      4, the exact LOD E/B update every step.
+  batch96 : 96 independent MHD domains, cube edges from {32,48,64,80,96}
+      (seed 3), a disk magnet each (radius 4..12, seed 4), one persistent
+      launch per step for all of them, autotuned launch shape, CUDA graph.
+  tgv64/256/384 : plain D3Q19 SRT FP32, periodic Taylor-Green vortex (u0 0.05).
+A step is one timestep of every cell (stream_collide, LOD bins, E/B update).
+Metric: MLUPs/s = cells * steps / seconds / 1e6.
 
-  value      : device time (CUDA events on the library's stream) of K steps
-               with all inputs resident in HBM.
-  e2e        : the same job through the C ABI with host buffers: upload of
-               the inputs from pinned memory, initialize, K steps (CUDA
-               graph), download of rho/u/Q/E/B, all inside the timed region.
-  roofline   : the dominant kernel (the E/B update, FP32-bound) against the
-               measured FP32 FMA peak; roofline_stencil: stream_collide
-               against the measured HBM bandwidth (MEASURED_PEAKS.json).
+  value       : CUDA-event time of K steps on the library's stream, inputs
+                resident in HBM.
+  e2e         : the same job through the C ABI with host buffers: upload of
+                the inputs from pinned memory, initialize, K steps (CUDA graph),
+                download of the result fields, inside the timed region.
+  roofline    : the dominant kernel -- the E/B update, FP32-bound -- against
+                the measured FP32 FMA peak (ion_probe_fp32_peak); the plain
+                workloads' dominant kernel is stream_collide against the
+                measured HBM bandwidth (MEASURED_PEAKS.json).
   cpu_baseline: the reference's kernels compiled for the host (or the C
-               restatement of them when the reference copy is absent), all
-               host cores, on a bounded sample of the same workload.
+                restatement when the reference copy is absent), all host cores,
+                a bounded sample of the same workload.
 
 ``--impl reference`` runs only that CPU implementation and prints its line.
-Multi-GPU (torchrun): replicas only -- every rank advances its own domain,
-no data exchange; value = cells * steps * ranks / max-over-ranks time.
+Multi-GPU (torchrun): replicas only -- every rank advances its own copy of the
+workload on its own GPU, no data exchange; value = ranks * cells * steps /
+max-over-ranks time.
 """
 from __future__ import annotations
 
 import argparse
+import datetime as _dt
 import json
 import os
 import statistics
@@ -40,12 +49,11 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-# Algorithmic bytes per lattice update (FP32 storage, D3Q19 + D3Q7 + electron gas):
-#   fi 19 loads + 19 stores, ei 19+19, fqi 7+7 (4 B each) = 360; E,B dyn 24;
-#   flags 1; Q 4; LOD velocity 12; rho,u 16 (update_fields)          -> 417
-BYTES_PER_LUP_MHD_FP32 = 417
-BYTES_PER_LUP_PLAIN_FP32 = 169  # 38 DDF accesses x 4 B + flags + rho,u
-FLOP_PER_INTERACTION = 34       # E and B from one source: 34 FLOP + 1 sqrt
+FLOP_PER_INTERACTION = 34  # one source's E and B: 34 FLOP + 1 sqrt (sim_kernels.cl:950-954)
+# kernel-time results of one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum per launch);
+# the summaries with the commands that produced them are in profiles/
+NCU_TRAFFIC = {("tgv256", "k_stream_collide"): 2.506905e9, ("mhd128", "k_stream_collide"): 0.797089e9,
+               ("mhd128", "k_update_e_b<fast>"): 59.139e6}
 
 
 def parse():
@@ -54,30 +62,68 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="mhd128", choices=["mhd128", "mhd256", "tgv64", "tgv256", "tgv384"])
+    p.add_argument("--workload", default="mhd128",
+                   choices=["mhd128", "mhd256", "mhd64", "batch96", "tgv64", "tgv256", "tgv384"])
     p.add_argument("--field-mode", default="fast", choices=["bitwise", "fast"])
+    p.add_argument("--float-type", default="FP32", choices=["FP32", "FP16S", "FP16C"])
     p.add_argument("--ref-seconds", type=float, default=20.0, help="CPU time budget of the reference/baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
     return p.parse_args()
 
 
-def make_case(workload: str, field_mode: str):
+FT = {"FP16S": 0, "FP16C": 1, "FP32": 2}
+
+
+def make_cases(a) -> list[dict]:
     from ionsolver_gb300 import workloads as W
-    fm = 0 if field_mode == "bitwise" else 1
-    if workload.startswith("mhd"):
-        n = int(workload[3:])
-        case = W.mhd_box(n=n, field_mode=fm, magnet_r=16.0 * n / 128, magnet_t=8.0 * n / 128)
-    else:
-        n = int(workload[3:])
-        case = W.taylor_green(n=n, amplitude=0.05)
-        case["config"]["update_fields"] = 0
-    return case
+    fm = 0 if a.field_mode == "bitwise" else 1
+    ft = FT[a.float_type]
+    w = a.workload
+    if w == "batch96":
+        return W.batch_domains(96, float_type=ft, field_mode=fm)
+    n = int(w[3:])
+    if w.startswith("mhd"):
+        return [W.mhd_box(n=n, float_type=ft, field_mode=fm, magnet_r=16.0 * n / 128, magnet_t=8.0 * n / 128)]
+    case = W.taylor_green(n=n, amplitude=0.05, float_type=ft)
+    case["config"]["update_fields"] = 0
+    return [case]
 
 
-# ---------------------------------------------------------------------------
-# distributed plumbing (replicas only)
+def bytes_per_lup(cfg: dict) -> int:
+    """Algorithmic DRAM bytes of one lattice update of stream_collide."""
+    db = 4 if cfg.get("float_type", 2) == 2 else 2
+    b = 2 * 19 * db + 1                      # DDFs loaded and stored once, flags
+    if cfg.get("update_fields"):
+        b += 16                              # rho, u written
+    if cfg.get("ext_magneto_hydro"):
+        b += 2 * (19 + 7) * db               # electron and charge DDFs
+        b += 24 + 4                          # E, B read; Q written
+        if cfg.get("mhd_lod_depth", 4) > 0:
+            b += 12                          # velocity contribution to the LOD bins
+    return b
+
+
+def field_interactions(cfg: dict, flags: np.ndarray) -> int:
+    """Source terms the E/B update evaluates (fluid cells x LOD bins in range, own bin excluded)."""
+    D = int(cfg["mhd_lod_depth"])
+    nd = 1 << D
+    n_own = 1 + sum(8 ** (i + 1) for i in range(D))
+    first = n_own - nd ** 3
+    nx, ny, nz = cfg["n_x"], cfg["n_y"], cfg["n_z"]
+    fl = ((flags & 0x1F) != 0x01).reshape(nz, ny, nx)
+    bz = (np.arange(nz) // (nz // nd))[:, None, None]
+    by = (np.arange(ny) // (ny // nd))[None, :, None]
+    bx = (np.arange(nx) // (nx // nd))[None, None, :]
+    own = bx + (by + bz * nd) * nd
+    fluid = int(fl.sum())
+    return fluid * (nd ** 3 - first) - int((fl & (own >= first)).sum())
+
+
 # ---------------------------------------------------------------------------
 class Dist:
+    """Rank bookkeeping; N > 1 runs independent replicas (gloo for barrier/max)."""
+
     def __init__(self):
         self.rank = int(os.environ.get("RANK", "0"))
         self.world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -106,18 +152,18 @@ class Dist:
             self.pg.destroy_process_group()
 
 
-# ---------------------------------------------------------------------------
-# clocks during the timed region
-# ---------------------------------------------------------------------------
 class Clocks:
-    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    """nvidia-smi samples every 200 ms; the summary uses the samples taken inside the timed window."""
+    QUERY = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
 
     def __init__(self, index: int):
         self.index = index
         self.proc = None
         self.path = ROOT / "gpurun_out" / f"clocks_rank{index}.csv"
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
@@ -126,69 +172,84 @@ class Clocks:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
                                           "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
+            time.sleep(0.5)
         except Exception:
             self.proc = None
+
+    def mark(self, which: str):
+        setattr(self, which, _dt.datetime.now())
 
     def stop(self) -> dict | None:
         if not self.proc:
             return None
+        time.sleep(0.3)
         self.proc.terminate()
         try:
             self.proc.wait(5)
         except Exception:
             self.proc.kill()
         self.f.close()
-        sm, smax, reasons = [], 0.0, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         for line in self.path.read_text().splitlines():
-            parts = [x.strip() for x in line.split(",")]
-            if len(parts) < 9:
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 8:
                 continue
             try:
-                sm.append(float(parts[1]))
-                smax = max(smax, float(parts[2]))
+                ts = _dt.datetime.strptime(p[0], "%Y/%m/%d %H:%M:%S.%f")
+                rows.append((ts, float(p[1]), float(p[2]), p[3], p[4:8]))
             except ValueError:
                 continue
-            for name, v in zip(names, parts[5:9]):
-                if v.lower() == "active":
-                    reasons.add(name)
-        if not sm:
+        if not rows:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        inside = [r for r in rows if self.t0 and self.t1 and self.t0 <= r[0] <= self.t1]
+        use = inside if inside else rows
+        reasons = sorted({n for r in use for n, v in zip(self.NAMES, r[4]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[1] for r in use), "sm_max_mhz": max(r[2] for r in use),
+                "reasons": reasons, "samples": len(use), "window": "timed region" if inside else "whole run"}
 
 
 # ---------------------------------------------------------------------------
-# CPU implementations (the reference's kernels on host cores, or the port)
-# ---------------------------------------------------------------------------
-def cpu_run(case, steps: int, budget_s: float, init_fields: dict | None):
-    """Advances the case on the host cores; returns (MLUPs/s, sample text, kind, cores)."""
+def cpu_run(cases: list[dict], steps: int, budget_s: float, init_fields: list[dict] | None):
+    """Advances the cases on the host cores within a time budget.
+
+    Returns (MLUPs/s, sample description, kind, cores)."""
     import oracle as O
     from tests import _util as U
     cores = O.cpu_count()
-    kind = "reference"
-    try:
-        if not O.reference_available():
-            raise RuntimeError("no reference copy")
-        o = O.OracleLbm(U.oracle_config(case), "ref", cores)
-    except Exception:
-        kind = "port"
-        o = O.OracleLbm(U.oracle_config(case), "f32", cores)
-    for name, arr in case["fields"].items():
-        o.set_field(name, arr)
-    for name, arr in (init_fields or {}).items():  # static field precomputed on the GPU (setup, untimed)
-        o.set_field(name, arr)
-    o.initialize()
-    N = o.n
-    done, t0 = 0, time.perf_counter()
-    while done < steps:
-        o.do_time_step()
-        done += 1
-        if time.perf_counter() - t0 > budget_s:
+    kind = "reference" if O.reference_available() else "port"
+    done_cells, done_steps, t_total, used = 0, 0, 0.0, 0
+    for i, case in enumerate(cases):
+        try:
+            o = O.OracleLbm(U.oracle_config(case), "ref" if kind == "reference" else "f32", cores)
+        except Exception:
+            kind = "port"
+            o = O.OracleLbm(U.oracle_config(case), "f32", cores)
+        for name, arr in case["fields"].items():
+            o.set_field(name, arr)
+        for name, arr in ((init_fields or [{}] * len(cases))[i] or {}).items():  # static fields (setup, untimed)
+            o.set_field(name, arr)
+        o.initialize()
+        t0 = time.perf_counter()
+        s = 0
+        while s < steps:
+            o.do_time_step()
+            s += 1
+            if t_total + time.perf_counter() - t0 > budget_s:
+                break
+        t_total += time.perf_counter() - t0
+        done_cells += o.n * s
+        done_steps += s
+        used += 1
+        o.close()
+        if t_total > budget_s:
             break
-    dt = time.perf_counter() - t0
-    mlups = N * done / dt / 1e6
-    sample = f"{done} full timestep(s) of the {case['config']['n_x']}^3 case after initialize, {dt:.1f} s wall"
+    mlups = done_cells / t_total / 1e6
+    if len(cases) == 1:
+        c = cases[0]["config"]
+        sample = (f"{done_steps} full timestep(s) of the {c['n_x']}x{c['n_y']}x{c['n_z']} case after initialize, "
+                  f"{t_total:.1f} s")
+    else:
+        sample = f"{done_steps} domain-step(s) over the first {used} of {len(cases)} domains, {t_total:.1f} s"
     return mlups, sample, kind, cores
 
 
@@ -196,27 +257,30 @@ def cpu_run(case, steps: int, budget_s: float, init_fields: dict | None):
 def main():
     a = parse()
     dist = Dist()
-    case = make_case(a.workload, a.field_mode)
-    c = case["config"]
-    N = c["n_x"] * c["n_y"] * c["n_z"]
-    mhd = bool(c.get("ext_magneto_hydro"))
-    workload_cfg = {"workload": a.workload, "cells": N, "size": [c["n_x"], c["n_y"], c["n_z"]],
-                    "velocity_set": "D3Q19", "float_type": "FP32", "relaxation": "SRT", "tau": 0.6,
-                    "mhd": mhd, "lod_depth": c.get("mhd_lod_depth") if mhd else None,
+    cases = make_cases(a)
+    cfg0 = cases[0]["config"]
+    mhd = bool(cfg0.get("ext_magneto_hydro"))
+    cells = sum(c["config"]["n_x"] * c["config"]["n_y"] * c["config"]["n_z"] for c in cases)
+    bpl = bytes_per_lup(cfg0)
+    workload_cfg = {"workload": a.workload, "cells": cells, "domains": len(cases),
+                    "size": [cfg0["n_x"], cfg0["n_y"], cfg0["n_z"]] if len(cases) == 1 else "uneven",
+                    "velocity_set": "D3Q19", "float_type": a.float_type, "relaxation": "SRT", "tau": 0.6,
+                    "mhd": mhd, "lod_depth": cfg0.get("mhd_lod_depth") if mhd else None,
                     "field_mode": a.field_mode if mhd else None,
-                    "l2": "working set (%.0f MB) larger than L2 (126 MB)" % (
-                        N * (BYTES_PER_LUP_MHD_FP32 if mhd else BYTES_PER_LUP_PLAIN_FP32) / 1e6),
+                    "update_fields": bool(cfg0.get("update_fields")),
+                    "l2": "working set %.0f MB > L2 (126 MB): no flush needed" % (cells * bpl / 1e6),
                     "parallelism": f"replicas x{dist.world}"}
     metric = "D3Q19-MHD MLUPs/s" if mhd else "D3Q19 MLUPs/s"
+    dtype = {"FP32": "f32", "FP16S": "f32 (FP16S storage)", "FP16C": "f32 (FP16C storage)"}[a.float_type]
 
     if a.impl == "reference":
         if dist.rank != 0:
             dist.close()
             return
-        mlups, sample, kind, cores = cpu_run(case, max(a.steps, 1), a.ref_seconds, None)
+        mlups, sample, kind, cores = cpu_run(cases, max(a.steps, 1), a.ref_seconds, None)
         line = {"metric": metric, "value": mlups, "unit": "MLUPs/s", "n_gpus": a.gpus, "steps": a.steps,
-                "warmup": a.warmup, "ms_per_step": N / mlups / 1e3, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_cfg,
+                "warmup": a.warmup, "ms_per_step": cells / mlups / 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": workload_cfg,
                 "impl": "reference",
                 "cpu_baseline": {"value": mlups, "unit": "MLUPs/s", "cores": cores, "kind": kind, "sample": sample},
                 "e2e": {"value": mlups, "unit": "MLUPs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -224,42 +288,54 @@ def main():
         dist.close()
         return
 
+    import ctypes as C
     import ionsolver_gb300 as I
     from ionsolver_gb300 import _native as NAT
     from ionsolver_gb300 import workloads as W
     NAT.check(NAT.lib().ion_select_device(dist.local))
 
-    lbm = I.Lbm(W.lbm_config(case))
-    W.apply_case(lbm, case)
-    lbm.initialize()
-    lbm.set_kernel_timing(True)
-    for _ in range(a.warmup):
-        lbm.do_time_step()
-    lbm.finish_queues(600000)
-    lbm.reset_kernel_time()
-
+    doms = []
+    for case in cases:
+        lbm = I.Lbm(W.lbm_config(case))
+        W.apply_case(lbm, case)
+        lbm.initialize()
+        doms.append(lbm)
+    batch = I.Batch(doms) if len(doms) > 1 else None
     clocks = Clocks(dist.local)
+    clocks.start()
+
+    # ---- warm-up, then K timed steps (device time, CUDA events) -----------------
+    if batch is None:
+        lbm = doms[0]
+        lbm.set_kernel_timing(True)
+        for _ in range(a.warmup):
+            lbm.do_time_step()
+        lbm.finish_queues(600000)
+        lbm.reset_kernel_time()
+    else:
+        batch.run(max(a.warmup, 1) + 2 * 4)  # includes the autotuner's trial steps
+        batch.finish(600000)
     launches0 = I.kernel_launch_count()
     dist.barrier()
-    lbm.finish_queues(600000)
-    clocks.start()
-    lbm.record_event(0)
-    for _ in range(a.steps):
-        lbm.do_time_step()
-    lbm.record_event(1)
-    ms = lbm.elapsed_ms(0, 1)
-    lbm.finish_queues(600000)
-    clk = clocks.stop()
+    clocks.mark("t0")
+    if batch is None:
+        lbm.record_event(0)
+        for _ in range(a.steps):
+            lbm.do_time_step()
+        lbm.record_event(1)
+        ms = lbm.elapsed_ms(0, 1)
+        lbm.finish_queues(600000)
+    else:
+        batch.record_event(0)
+        batch.run(a.steps)
+        batch.record_event(1)
+        ms = batch.elapsed_ms(0, 1)
+        batch.finish(600000)
+    clocks.mark("t1")
     launches = I.kernel_launch_count() - launches0
     dist.barrier()
     ms_max = dist.max(ms)
-    value = N * a.steps * dist.world / (ms_max * 1e-3) / 1e6
-
-    sc_ms, sc_n = lbm.kernel_time(0)
-    eb_ms, eb_n = lbm.kernel_time(1)
-    bins_ms, bins_n = lbm.kernel_time(2)
-    flags = lbm.read("flags")
-    fluid = int(((flags & 0x1F) != 0x01).sum())
+    value = cells * a.steps * dist.world / (ms_max * 1e-3) / 1e6
 
     peaks = {}
     try:
@@ -267,99 +343,111 @@ def main():
     except Exception:
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    hbm_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    bpl = BYTES_PER_LUP_MHD_FP32 if mhd else BYTES_PER_LUP_PLAIN_FP32
-    sc_avg = sc_ms / max(sc_n, 1)
-    stencil_gbs = N * bpl / (sc_avg * 1e-3) / 1e9
-    roof_stencil = {"bound": "hbm", "achieved": stencil_gbs, "peak": hbm_peak, "unit": "GB/s",
-                    "frac": stencil_gbs / hbm_peak, "traffic": None, "kernel": "k_stream_collide",
-                    "bytes_per_lup": bpl, "peak_source": hbm_src, "avg_launch_ms": sc_avg}
-    roofline = roof_stencil
-    if mhd:
-        import ctypes as C
-        tf = C.c_double()
-        NAT.check(NAT.lib().ion_probe_fp32_peak(C.byref(tf)))
-        # sources per fluid cell: the depth-4 bins [585, 4096) minus the cell's own bin when it is among them
-        nd = 1 << c["mhd_lod_depth"]
-        n_own = 1 + sum(8 ** (i + 1) for i in range(c["mhd_lod_depth"]))
-        first = n_own - nd ** 3
-        bs = c["n_x"] // nd
-        z_first = first // (nd * nd)  # bins below `first` are whole z-layers plus part of one
-        own_in = fluid - sum(1 for _ in range(0))  # refined below
-        fl3 = ((flags & 0x1F) != 0x01).reshape(c["n_z"], c["n_y"], c["n_x"])
-        zb = np.arange(c["n_z"]) // bs
-        yb = np.arange(c["n_y"]) // bs
-        xb = np.arange(c["n_x"]) // bs
-        own = xb[None, None, :] + (yb[None, :, None] + zb[:, None, None] * nd) * nd
-        own_in = int((fl3 & (own >= first)).sum())
-        interactions = fluid * (nd ** 3 - first) - own_in
-        eb_avg = eb_ms / max(eb_n, 1)
-        tflops = interactions * FLOP_PER_INTERACTION / (eb_avg * 1e-3) / 1e12
-        roofline = {"bound": "fp32", "achieved": tflops, "peak": tf.value, "unit": "TFLOP/s",
-                    "frac": tflops / tf.value, "traffic": None, "kernel": "k_update_e_b<%s>" % a.field_mode,
-                    "flop_per_launch": interactions * FLOP_PER_INTERACTION, "avg_launch_ms": eb_avg,
-                    "peak_source": "measured FP32 FMA probe (ion_probe_fp32_peak)", "z_first_layer": z_first}
-        share = {"update_e_b": eb_ms, "stream_collide": sc_ms, "lod_bins": bins_ms}
-    else:
-        share = {"stream_collide": sc_ms}
-
-    # ---- end to end through the C ABI with host buffers -----------------------------
-    lbm.set_kernel_timing(False)
-    e2e = None
-    try:
-        import torch
-        ins = {k: v for k, v in case["fields"].items()}
+    hbm_src = "measured (MEASURED_PEAKS.json)" if "hbm_gbs" in peaks else "fallback"
+    share, roof_stencil, roofline, extra = {}, None, None, {}
+    if batch is None:
+        sc_ms, sc_n = lbm.kernel_time(0)
+        eb_ms, eb_n = lbm.kernel_time(1)
+        bins_ms, _ = lbm.kernel_time(2)
+        sc_avg = sc_ms / max(sc_n, 1)
+        gbs = cells * bpl / (sc_avg * 1e-3) / 1e9
+        tr = NCU_TRAFFIC.get((a.workload, "k_stream_collide"))
+        roof_stencil = {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                        "traffic": tr, "kernel": "k_stream_collide", "bytes_per_lup": bpl,
+                        "bytes_per_launch": cells * bpl, "avg_launch_ms": sc_avg, "peak_source": hbm_src}
+        share = {"stream_collide_ms": sc_ms}
+        roofline = roof_stencil
         if mhd:
-            ins["b_stat"] = lbm.read("b_stat")
-            ins["flags"] = flags
-        pinned = {}
-        for k, v in ins.items():
-            t = torch.empty(v.size, dtype=torch.from_numpy(v[:1]).dtype, pin_memory=True)
-            t.numpy()[:] = v
-            pinned[k] = t
-        outs = ["rho", "u"] + (["q", "e_dyn", "b_dyn"] if mhd else [])
-        out_pinned = {}
-        for k in outs:
-            eb, cnt = lbm.field_info(k)
-            out_pinned[k] = torch.empty(cnt, dtype=torch.uint8 if k == "flags" else torch.float32, pin_memory=True)
-        lib = NAT.lib()
-        h = lbm.handle
-        e2e_lbm = lbm
-        h2d = sum(t.numel() * t.element_size() for t in pinned.values())
-        d2h = sum(t.numel() * t.element_size() for t in out_pinned.values())
-        dist.barrier()
-        e2e_lbm.finish_queues(600000)
-        t0 = time.perf_counter()
-        for k, t in pinned.items():
-            NAT.check(lib.ion_lbm_write_field(h, I.FIELDS[k], t.data_ptr(), t.numel() * t.element_size()))
-        NAT.check(lib.ion_lbm_initialize(h))
-        NAT.check(lib.ion_lbm_run(h, a.steps))
-        for k, t in out_pinned.items():
-            NAT.check(lib.ion_lbm_read_field(h, I.FIELDS[k], t.data_ptr(), t.numel() * t.element_size()))
-        dt = time.perf_counter() - t0
-        dt = dist.max(dt)
-        e2e = {"value": N * a.steps * dist.world / dt / 1e6, "unit": "MLUPs/s",
-               "h2d_bytes_per_step": h2d / a.steps, "d2h_bytes_per_step": d2h / a.steps,
-               "path": "ion_lbm_write_field x%d, ion_lbm_initialize, ion_lbm_run(%d), ion_lbm_read_field x%d"
-                       % (len(pinned), a.steps, len(out_pinned))}
-    except Exception as ex:  # e2e is reported as missing rather than faked
-        e2e = {"value": None, "unit": "MLUPs/s", "error": str(ex)[:200]}
+            share.update(update_e_b_ms=eb_ms, lod_bins_ms=bins_ms)
+    tf = C.c_double()
+    if mhd:
+        NAT.check(NAT.lib().ion_probe_fp32_peak(C.byref(tf)))
+        inter = sum(field_interactions(c["config"], d.read("flags")) for c, d in zip(cases, doms))
+        if batch is None:
+            avg = eb_ms / max(eb_n, 1)
+            kname = f"k_update_e_b<{a.field_mode}>"
+        else:
+            avg = ms / a.steps
+            kname = f"k_batch_step<{a.field_mode}> (whole step; FLOPs of its E/B phase)"
+        tflops = inter * FLOP_PER_INTERACTION / (avg * 1e-3) / 1e12
+        roofline = {"bound": "fp32", "achieved": tflops, "peak": tf.value, "unit": "TFLOP/s",
+                    "frac": tflops / tf.value, "traffic": NCU_TRAFFIC.get((a.workload, kname)), "kernel": kname,
+                    "flop_per_launch": inter * FLOP_PER_INTERACTION, "interactions_per_launch": inter,
+                    "avg_launch_ms": avg, "peak_source": "measured FP32 FMA throughput (ion_probe_fp32_peak)"}
+    if batch is not None:
+        extra["autotuner"] = {"chosen": batch.chosen(), "trials": batch.tuning()}
+
+    # ---- end to end through the C ABI with host buffers ----------------------------
+    e2e = None
+    if not a.no_e2e:
+        try:
+            import torch
+            lib = NAT.lib()
+            jobs, h2d, d2h = [], 0, 0
+            for case, d in zip(cases, doms):
+                d.set_kernel_timing(False)
+                ins = dict(case["fields"])
+                if mhd:
+                    ins["b_stat"] = d.read("b_stat")
+                    ins["flags"] = d.read("flags")
+                pin_in = {}
+                for k, v in ins.items():
+                    t = torch.empty(v.size, dtype=torch.from_numpy(v[:1]).dtype, pin_memory=True)
+                    t.numpy()[:] = v
+                    pin_in[k] = t
+                pin_out = {}
+                for k in ["rho", "u"] + (["q", "e_dyn", "b_dyn"] if mhd else []):
+                    pin_out[k] = torch.empty(d.field_info(k)[1], dtype=torch.float32, pin_memory=True)
+                jobs.append((d, pin_in, pin_out))
+                h2d += sum(t.numel() * t.element_size() for t in pin_in.values())
+                d2h += sum(t.numel() * t.element_size() for t in pin_out.values())
+            dist.barrier()
+            for d in doms:
+                d.finish_queues(600000)
+            t0 = time.perf_counter()
+            for d, pin_in, _ in jobs:
+                for k, t in pin_in.items():
+                    NAT.check(lib.ion_lbm_write_field(d.handle, I.FIELDS[k], t.data_ptr(), t.numel() * t.element_size()))
+                NAT.check(lib.ion_lbm_initialize(d.handle))
+            if batch is None:
+                NAT.check(lib.ion_lbm_run(doms[0].handle, a.steps))
+            else:
+                batch.run(a.steps)
+                batch.finish(600000)
+            for d, _, pin_out in jobs:
+                for k, t in pin_out.items():
+                    NAT.check(lib.ion_lbm_read_field(d.handle, I.FIELDS[k], t.data_ptr(), t.numel() * t.element_size()))
+            dt = dist.max(time.perf_counter() - t0)
+            path = ("ion_lbm_write_field, ion_lbm_initialize, " +
+                    ("ion_lbm_run(K)" if batch is None else "ion_batch_run(K)") + ", ion_lbm_read_field")
+            e2e = {"value": cells * a.steps * dist.world / dt / 1e6, "unit": "MLUPs/s",
+                   "h2d_bytes_per_step": h2d / a.steps, "d2h_bytes_per_step": d2h / a.steps, "path": path}
+        except Exception as ex:  # reported as missing rather than faked
+            e2e = {"value": None, "unit": "MLUPs/s", "error": str(ex)[:200]}
+    clk = clocks.stop()
 
     cpu = None
     if dist.rank == 0 and not a.no_cpu_baseline:
-        init = {"b_stat": lbm.read("b_stat"), "flags": flags} if mhd else None
-        mlups, sample, kind, cores = cpu_run(case, 1000, a.ref_seconds, init)
+        init = [({"b_stat": d.read("b_stat"), "flags": d.read("flags")} if mhd else {}) for d in doms]
+        mlups, sample, kind, cores = cpu_run(cases, 10 ** 6, a.ref_seconds, init)
         cpu = {"value": mlups, "unit": "MLUPs/s", "cores": cores, "kind": kind, "sample": sample}
 
     if dist.rank == 0:
         line = {"metric": metric, "value": value, "unit": "MLUPs/s", "n_gpus": dist.world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, no dataset)",
-                "config": workload_cfg, "roofline": roofline, "roofline_stencil": roof_stencil,
-                "kernel_ms_in_timed_region": share, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clk}
+                "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded, no dataset)",
+                "config": workload_cfg, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": launches, "clocks": clk}
+        if roof_stencil is not None and roofline is not roof_stencil:
+            line["roofline_stencil"] = roof_stencil
+        if share:
+            line["kernel_ms_in_timed_region"] = share
+        line.update(extra)
         print(json.dumps(line), flush=True)
-    lbm.close()
+    if batch is not None:
+        batch.close()
+    for d in doms:
+        d.close()
     dist.close()
 
 

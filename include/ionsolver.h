@@ -238,6 +238,27 @@ int ion_lbm_set_kernel_timing(ion_lbm* h, int enable);
 int ion_lbm_kernel_time(ion_lbm* h, int kernel, double* total_ms, uint64_t* launches);
 int ion_lbm_reset_kernel_time(ion_lbm* h);
 
+/* ---- batches of independent domains (no reference counterpart; the
+ *      reference advances one domain per OpenCL queue, src/lbm/mod.rs:250-272)
+ *      Every domain of a batch keeps its own buffers, size, units and flags;
+ *      all must be D3Q19 with the same float type, MHD switch and field mode,
+ *      at time steps of equal parity.  One cooperative launch per step
+ *      advances all of them (stream_collide, LOD bins, E/B); results equal
+ *      stepping each domain alone. ----------------------------------------- */
+typedef struct ion_batch ion_batch;
+int ion_batch_create(ion_lbm* const* domains, uint32_t count, ion_batch** out);
+int ion_batch_destroy(ion_batch* b);
+/* Advances every domain by `steps`.  The first call autotunes the launch
+ * shape on its first steps (each candidate shape runs two real steps) and
+ * then replays a CUDA graph of two steps. Asynchronous. */
+int ion_batch_run(ion_batch* b, uint64_t steps);
+/* bounded wait for the batch's stream; reports device-side timeouts */
+int ion_batch_finish(ion_batch* b, int timeout_ms);
+/* autotuner record i (block, grid, ms per step); i = 0xFFFFFFFF: the chosen shape */
+int ion_batch_tuning(ion_batch* b, uint32_t i, uint32_t* block, uint32_t* grid, float* ms_per_step);
+int ion_batch_record_event(ion_batch* b, int slot);
+int ion_batch_event_elapsed(ion_batch* b, int start, int end, float* ms);
+
 /* ---- storage codecs on the device (no reference counterpart; exposes the
  *      FP16S/FP16C codecs of src/lbm/domain.rs:773-780 and
  *      src/kernels/sim_kernels.cl:79-90 for exhaustive checks) ------------ */

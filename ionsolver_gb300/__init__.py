@@ -4,7 +4,7 @@ The compute path is libionsolver.so (hand-written sm_103a CUDA kernels plus a
 C++ host library behind the C ABI of include/ionsolver.h).  This package is
 the Python mirror of the reference's Rust API over that ABI.
 """
-from .lbm import (FIELDS, FieldMode, FloatType, Lbm, LbmConfig, ModelType, RelaxationTime, Units, VelocitySet,
+from .lbm import (FIELDS, Batch, FieldMode, FloatType, Lbm, LbmConfig, ModelType, RelaxationTime, Units, VelocitySet,
                   codec_roundtrip, kernel_launch_count, taylor_green_fields)
 from .meshes import annulus, cylinder
 from ._native import IonError, LIB_PATH

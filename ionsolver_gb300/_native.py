@@ -93,6 +93,14 @@ _SIGS = {
     "ion_lbm_kernel_time": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
     "ion_lbm_reset_kernel_time": (C.c_int, [_P]),
     "ion_codec_roundtrip": (C.c_int, [C.c_int, _P, _P, _P, _P, _P, C.c_uint64]),
+    "ion_batch_create": (C.c_int, [C.POINTER(_P), C.c_uint32, C.POINTER(_P)]),
+    "ion_batch_destroy": (C.c_int, [_P]),
+    "ion_batch_run": (C.c_int, [_P, C.c_uint64]),
+    "ion_batch_finish": (C.c_int, [_P, C.c_int]),
+    "ion_batch_tuning": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                   C.POINTER(C.c_float)]),
+    "ion_batch_record_event": (C.c_int, [_P, C.c_int]),
+    "ion_batch_event_elapsed": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(C.c_float)]),
 }
 
 _lib: C.CDLL | None = None

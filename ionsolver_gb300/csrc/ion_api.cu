@@ -4,6 +4,8 @@
 // (src/lbm/mod.rs, src/lbm/domain.rs, src/mesh.rs, src/file.rs,
 // src/lbm/units.rs); kernels in lbm_q*.cu, field_kernels.cu,
 // setup_kernels.cu.  Nothing here computes physics on the CPU.
+#include <algorithm>
+#include <array>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -483,7 +485,7 @@ int ion_lbm_create(const ion_config* cfg, ion_lbm** out) {
     L.w = h->k.w; L.ke = h->k.ke; L.kmu = h->k.kmu; L.kmu0 = h->k.kmu0; L.kkge = h->k.kkge; L.wq = h->k.wq;
     L.fx = cfg->f_x; L.fy = cfg->f_y; L.fz = cfg->f_z;
     L.ext_eq = cfg->ext_equilibrium_boundaries; L.ext_vf = cfg->ext_volume_force; L.ext_ff = cfg->ext_force_field;
-    L.ext_mhd = mhd; L.update_fields = cfg->update_fields;
+    L.ext_mhd = mhd; L.update_fields = cfg->update_fields; L.trt = cfg->relaxation_time == ION_TRT;
     L.depth = depth; L.nd = nd; L.n_lod_own = n_lod_own;
     L.n_bins = nd * nd * nd;
     L.first_src = n_lod_own > L.n_bins ? n_lod_own - L.n_bins : 0u;
@@ -986,6 +988,271 @@ int ion_lbm_reset_kernel_time(ion_lbm* h) {
     int rc = ion_lbm_kernel_time(h, 0, &d, &c);
     if (rc) return rc;
     for (int i = 0; i < 3; i++) { h->ktime[i] = 0; h->kcount[i] = 0; }
+    return ION_OK;
+}
+
+// ---- batches of independent domains (batch_kernels.cu) -----------------------
+}  // extern "C"
+
+struct ion_batch {
+    std::vector<ion_lbm*> doms;
+    int ft = ION_FP32;
+    bool mhd = false, fast = false;
+    cudaStream_t stream = nullptr;
+    DevLbm* d_doms = nullptr;
+    uint32_t* d_tile_off[3] = {nullptr, nullptr, nullptr};  // block 128, 256, 512
+    uint32_t total_tiles[3] = {0, 0, 0};
+    uint32_t* d_bin_off = nullptr;
+    uint32_t total_bins = 0;
+    uint32_t* d_sync = nullptr;  // [0] barrier count, [1] barrier generation, [2] error
+    uint64_t t = 0;
+    int sms = 0;
+    bool tuned = false;
+    uint32_t block = 256, grid = 0;
+    std::vector<std::array<float, 3>> tuning;  // block, grid, ms per step
+    cudaGraphExec_t graph = nullptr;
+    bool graph_failed = false;
+    cudaEvent_t ev[4] = {};
+    std::vector<void*> allocs;
+};
+
+namespace {
+
+const uint32_t kBatchBlocks[2] = {128, 256};
+
+int block_slot(uint32_t block) { return block == 128 ? 0 : block == 256 ? 1 : 2; }
+
+BatchDev batch_view(ion_batch* b, uint32_t block) {
+    BatchDev B{};
+    B.doms = b->d_doms;
+    B.ndom = (uint32_t)b->doms.size();
+    B.tile_off = b->d_tile_off[block_slot(block)];
+    B.total_tiles = b->total_tiles[block_slot(block)];
+    B.bin_off = b->d_bin_off;
+    B.total_bins = b->total_bins;
+    B.bar_count = b->d_sync;
+    B.bar_gen = b->d_sync + 1;
+    B.err = b->d_sync + 2;
+    return B;
+}
+
+int batch_launch(ion_batch* b, uint32_t block, uint32_t grid) {
+    const cudaError_t e = launch_batch_step(batch_view(b, block), b->ft, b->mhd, b->fast, grid, block, b->t, b->stream);
+    if (e != cudaSuccess) return fail(ION_E_CUDA, "batch step launch: %s", cudaGetErrorString(e));
+    g_launches++;
+    b->t += 1;
+    return ION_OK;
+}
+
+void destroy_batch(ion_batch* b) {
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (void* p : b->allocs) cudaFree(p);
+    for (auto& e : b->ev) if (e) cudaEventDestroy(e);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ion_batch_create(ion_lbm* const* domains, uint32_t count, ion_batch** out) {
+    if (!domains || !out || count == 0) return fail(ION_E_INVALID, "empty batch");
+    *out = nullptr;
+    ion_lbm* d0 = domains[0];
+    for (uint32_t i = 0; i < count; i++) {
+        ion_lbm* h = domains[i];
+        if (!h) return fail(ION_E_INVALID, "null domain %u", i);
+        if (h->q != 19) return fail(ION_E_CONFIG, "batches run D3Q19 domains");
+        if (h->cfg.float_type != d0->cfg.float_type || h->cfg.ext_magneto_hydro != d0->cfg.ext_magneto_hydro ||
+            (h->cfg.ext_magneto_hydro && h->cfg.field_mode != d0->cfg.field_mode))
+            return fail(ION_E_CONFIG, "domain %u differs from domain 0 in float type, MHD or field mode", i);
+        for (uint32_t k = 0; k < i; k++)
+            if (domains[k] == h) return fail(ION_E_INVALID, "domain %u appears twice", i);
+    }
+    for (uint32_t i = 0; i < count; i++) {
+        ion_lbm* h = domains[i];
+        if (!h->initialized) {
+            int rc = ion_lbm_initialize(h);
+            if (rc) return rc;
+        }
+        CK(cudaStreamSynchronize(h->stream));
+        if ((h->t & 1u) != (d0->t & 1u)) return fail(ION_E_STATE, "domains must be at time steps of equal parity");
+    }
+    ion_batch* b = new ion_batch();
+    b->doms.assign(domains, domains + count);
+    b->ft = d0->cfg.float_type;
+    b->mhd = d0->cfg.ext_magneto_hydro;
+    b->fast = b->mhd && d0->cfg.field_mode == ION_FIELD_FAST;
+    b->t = d0->t;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete b;
+        return fail(ION_E_CUDA, "cudaStreamCreate failed");
+    }
+    auto dalloc = [&](void** p, size_t bytes) -> int {
+        if (cudaMalloc(p, bytes) != cudaSuccess) { cudaGetLastError(); return fail(ION_E_NOMEM, "batch tables"); }
+        b->allocs.push_back(*p);
+        return ION_OK;
+    };
+    std::vector<DevLbm> views(count);
+    std::vector<uint32_t> bins(count + 1, 0);
+    for (uint32_t i = 0; i < count; i++) {
+        views[i] = domains[i]->L;
+        bins[i + 1] = bins[i] + (b->mhd ? domains[i]->L.n_lod_own : 0u);
+    }
+    b->total_bins = bins[count];
+    int rc = dalloc((void**)&b->d_doms, sizeof(DevLbm) * count);
+    if (!rc) rc = dalloc((void**)&b->d_bin_off, sizeof(uint32_t) * (count + 1));
+    if (!rc) rc = dalloc((void**)&b->d_sync, sizeof(uint32_t) * 4);
+    for (int s = 0; s < 2 && !rc; s++) {
+        std::vector<uint32_t> tiles(count + 1, 0);
+        const uint32_t per = kBatchBlocks[s] * EB_CPT;  // cells per tile
+        for (uint32_t i = 0; i < count; i++) tiles[i + 1] = tiles[i] + (domains[i]->L.n + per - 1) / per;
+        b->total_tiles[s] = tiles[count];
+        rc = dalloc((void**)&b->d_tile_off[s], sizeof(uint32_t) * (count + 1));
+        if (!rc && cudaMemcpy(b->d_tile_off[s], tiles.data(), sizeof(uint32_t) * (count + 1), cudaMemcpyHostToDevice) != cudaSuccess)
+            rc = fail(ION_E_CUDA, "batch table upload");
+    }
+    if (!rc && (cudaMemcpy(b->d_doms, views.data(), sizeof(DevLbm) * count, cudaMemcpyHostToDevice) != cudaSuccess ||
+                cudaMemcpy(b->d_bin_off, bins.data(), sizeof(uint32_t) * (count + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+                cudaMemset(b->d_sync, 0, sizeof(uint32_t) * 4) != cudaSuccess))
+        rc = fail(ION_E_CUDA, "batch table upload");
+    if (rc) { destroy_batch(b); return rc; }
+    for (auto& e : b->ev) cudaEventCreate(&e);
+    *out = b;
+    return ION_OK;
+}
+
+int ion_batch_destroy(ion_batch* b) {
+    destroy_batch(b);
+    return ION_OK;
+}
+
+// Autotuner: on the first run every launch shape (threads per block x blocks
+// per SM that fit on the SM) advances the batch by two real steps, timed with
+// CUDA events; the fastest shape is kept.  Results do not depend on the shape,
+// so the tuning steps are ordinary steps of the simulation.
+static int batch_autotune(ion_batch* b, uint64_t& steps) {
+    float best = 1e30f;
+    for (uint32_t block : kBatchBlocks) {
+        const int maxb = batch_max_blocks_per_sm(b->ft, b->mhd, b->fast, (int)block);
+        for (int bps = 1; bps <= std::min(maxb, 4); bps++) {
+            if (steps < 2) break;
+            const uint32_t grid = (uint32_t)(bps * b->sms);
+            CK(cudaEventRecord(b->ev[0], b->stream));
+            int rc = batch_launch(b, block, grid);
+            if (!rc) rc = batch_launch(b, block, grid);
+            if (rc) return rc;
+            CK(cudaEventRecord(b->ev[1], b->stream));
+            CK(cudaEventSynchronize(b->ev[1]));
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
+            steps -= 2;
+            b->tuning.push_back({(float)block, (float)grid, ms / 2.0f});
+            if (ms < best) { best = ms; b->block = block; b->grid = grid; }
+        }
+    }
+    if (b->grid == 0) {  // not enough steps to tune: the middle shape
+        b->block = 256;
+        b->grid = (uint32_t)(std::max(1, std::min(2, batch_max_blocks_per_sm(b->ft, b->mhd, b->fast, 256))) * b->sms);
+    } else {
+        b->tuned = true;
+    }
+    return ION_OK;
+}
+
+int ion_batch_run(ion_batch* b, uint64_t steps) {
+    if (!b) return fail(ION_E_INVALID, "null batch");
+    const uint64_t total = steps;
+    if (!b->tuned) {
+        int rc = batch_autotune(b, steps);
+        if (rc) return rc;
+    }
+    if ((b->t & 1u) && steps) {
+        int rc = batch_launch(b, b->block, b->grid);
+        if (rc) return rc;
+        steps--;
+    }
+    if (steps >= 4 && !b->graph && !b->graph_failed) {
+        cudaGraph_t g;
+        bool ok = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+            const uint64_t t0 = b->t;
+            const cudaError_t e1 = launch_batch_step(batch_view(b, b->block), b->ft, b->mhd, b->fast, b->grid, b->block, 0, b->stream);
+            const cudaError_t e2 = launch_batch_step(batch_view(b, b->block), b->ft, b->mhd, b->fast, b->grid, b->block, 1, b->stream);
+            const cudaError_t e3 = cudaStreamEndCapture(b->stream, &g);
+            b->t = t0;
+            ok = e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess &&
+                 cudaGraphInstantiate(&b->graph, g, 0) == cudaSuccess;
+            if (e3 == cudaSuccess) cudaGraphDestroy(g);
+        }
+        if (!ok) { b->graph = nullptr; b->graph_failed = true; cudaGetLastError(); }
+    }
+    if (b->graph) {
+        for (; steps >= 2; steps -= 2) {
+            CK(cudaGraphLaunch(b->graph, b->stream));
+            g_launches += 2;
+            b->t += 2;
+        }
+    }
+    for (; steps > 0; steps--) {
+        int rc = batch_launch(b, b->block, b->grid);
+        if (rc) return rc;
+    }
+    for (ion_lbm* h : b->doms) h->t += total;
+    return ION_OK;
+}
+
+int ion_batch_finish(ion_batch* b, int timeout_ms) {
+    if (!b) return fail(ION_E_INVALID, "null batch");
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        const cudaError_t e = cudaStreamQuery(b->stream);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady) return fail(ION_E_CUDA, "batch stream: %s", cudaGetErrorString(e));
+        if (timeout_ms >= 0 && std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(timeout_ms))
+            return fail(ION_E_TIMEOUT, "batch still busy after %d ms", timeout_ms);
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    uint32_t err = 0;
+    CK(cudaMemcpy(&err, b->d_sync + 2, 4, cudaMemcpyDeviceToHost));
+    if (err) {
+        cudaMemset(b->d_sync, 0, 4 * sizeof(uint32_t));
+        return fail(ION_E_TIMEOUT, err == 2 ? "batch grid barrier timed out" : "batch field tile did not arrive in time");
+    }
+    return ION_OK;
+}
+
+int ion_batch_tuning(ion_batch* b, uint32_t i, uint32_t* block, uint32_t* grid, float* ms_per_step) {
+    if (!b) return fail(ION_E_INVALID, "null batch");
+    if (i == 0xFFFFFFFFu) {  // the chosen shape
+        if (block) *block = b->block;
+        if (grid) *grid = b->grid;
+        if (ms_per_step) *ms_per_step = 0.0f;
+        return b->tuned ? ION_OK : fail(ION_E_STATE, "not tuned yet");
+    }
+    if (i >= b->tuning.size()) return fail(ION_E_INVALID, "no tuning entry %u", i);
+    if (block) *block = (uint32_t)b->tuning[i][0];
+    if (grid) *grid = (uint32_t)b->tuning[i][1];
+    if (ms_per_step) *ms_per_step = b->tuning[i][2];
+    return ION_OK;
+}
+
+int ion_batch_record_event(ion_batch* b, int slot) {
+    if (!b || slot < 0 || slot >= 4) return fail(ION_E_INVALID, "bad event slot");
+    CK(cudaEventRecord(b->ev[slot], b->stream));
+    return ION_OK;
+}
+
+int ion_batch_event_elapsed(ion_batch* b, int a, int c, float* ms) {
+    if (!b || !ms || a < 0 || a >= 4 || c < 0 || c >= 4) return fail(ION_E_INVALID, "bad event slot");
+    CK(cudaEventSynchronize(b->ev[c]));
+    CK(cudaEventElapsedTime(ms, b->ev[a], b->ev[c]));
     return ION_OK;
 }
 

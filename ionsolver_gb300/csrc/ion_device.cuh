@@ -181,7 +181,7 @@ struct DevLbm {
     uint32_t bsx, bsy, bsz;      // LOD bin extent in cells
     uint32_t near_x, near_y, near_z;  // near-field block extent
     float ils;
-    uint8_t ext_eq, ext_vf, ext_ff, ext_mhd, update_fields;
+    uint8_t ext_eq, ext_vf, ext_ff, ext_mhd, update_fields, trt;
 };
 
 __device__ __forceinline__ void cell_xyz(const DevLbm& L, uint32_t n, uint32_t& x, uint32_t& y, uint32_t& z) {

@@ -25,6 +25,26 @@ struct VoxArgs {
 
 constexpr unsigned RED_BLOCK = 256;
 
+// Cells per thread of the E/B update: each staged source is applied to
+// EB_CPT cells held in registers (cells tile + threadIdx.x + k*blockDim.x).
+constexpr uint32_t EB_CPT = 2;
+
+// device view of a batch of domains (batch_kernels.cu)
+struct BatchDev {
+    const DevLbm* doms;
+    uint32_t ndom;
+    const uint32_t* tile_off;  // [ndom+1] prefix sums of ceil(n / blockDim)
+    uint32_t total_tiles;
+    const uint32_t* bin_off;   // [ndom+1] prefix sums of n_lod_own
+    uint32_t total_bins;
+    uint32_t* bar_count;
+    uint32_t* bar_gen;
+    uint32_t* err;
+};
+int batch_max_blocks_per_sm(int ft, bool mhd, bool fast, int block);
+cudaError_t launch_batch_step(const BatchDev& B, int ft, bool mhd, bool fast, uint32_t grid, uint32_t block,
+                              uint64_t t, cudaStream_t s);
+
 // per velocity set (lbm_q19.cu, lbm_q15.cu, lbm_q9.cu)
 #define ION_DECLARE_LBM_DISPATCH(NAME)                                                                    \
     void NAME##_stream_collide(const DevLbm& L, int ft, bool mhd, bool trt, uint64_t t, cudaStream_t s);  \

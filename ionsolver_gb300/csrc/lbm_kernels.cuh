@@ -252,15 +252,14 @@ __device__ __forceinline__ void trt_store(typename D::T* f, uint32_t N, uint32_t
 // stream_collide, one step (sim_kernels.cl:465-758)
 // ---------------------------------------------------------------------------
 template <int Q, int FT, bool MHD, bool TRT>
-__global__ void __launch_bounds__(256, MHD ? 2 : 3) k_stream_collide(const DevLbm L, const uint32_t odd_t) {
+__device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const bool odd) {
     using V = VSet<Q>;
     using D = Ddf<FT>;
     using T = typename D::T;
     const uint32_t N = L.n;
-    const bool odd = odd_t != 0u;
-    for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+    {
         const uint8_t fbo = L.flags[n] & F_BO;
-        if (fbo == F_S) continue;
+        if (fbo == F_S) return;
         const bool eqc = L.ext_eq && fbo == F_E;
         uint32_t x, y, z;
         cell_xyz(L, n, x, y, z);
@@ -346,6 +345,13 @@ __global__ void __launch_bounds__(256, MHD ? 2 : 3) k_stream_collide(const DevLb
         if constexpr (TRT) trt_store<V, D>((T*)L.fi, N, n, odd, j, fhn, es, fs, L.ext_vf, w, eqc);
         else srt_store<V, D>((T*)L.fi, N, n, odd, j, fhn, es, fs, L.ext_vf, c_tau, w, eqc);
     }
+}
+
+template <int Q, int FT, bool MHD, bool TRT>
+__global__ void __launch_bounds__(256, MHD ? 2 : 4) k_stream_collide(const DevLbm L, const uint32_t odd_t) {
+    const bool odd = odd_t != 0u;
+    for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < L.n; n += gridDim.x * blockDim.x)
+        sc_cell<Q, FT, MHD, TRT>(L, n, odd);
 }
 
 // ---------------------------------------------------------------------------

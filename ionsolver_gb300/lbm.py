@@ -356,6 +356,56 @@ class Lbm:
         N.check(N.lib().ion_lbm_reset_kernel_time(self._h))
 
 
+class Batch:
+    """Independent D3Q19 domains of uneven size advanced together, one
+    persistent launch per timestep (ion_batch_* of include/ionsolver.h)."""
+
+    def __init__(self, domains: Sequence[Lbm]):
+        self.domains = list(domains)
+        arr = (C.c_void_p * len(self.domains))(*[d.handle.value for d in self.domains])
+        self._h = C.c_void_p()
+        N.check(N.lib().ion_batch_create(arr, len(self.domains), C.byref(self._h)))
+
+    def run(self, steps: int) -> None:
+        N.check(N.lib().ion_batch_run(self._h, int(steps)))
+
+    def finish(self, timeout_ms: int = -1) -> None:
+        N.check(N.lib().ion_batch_finish(self._h, int(timeout_ms)))
+
+    def tuning(self) -> list[tuple[int, int, float]]:
+        out, i = [], 0
+        while True:
+            b, g, ms = C.c_uint32(), C.c_uint32(), C.c_float()
+            if N.lib().ion_batch_tuning(self._h, i, C.byref(b), C.byref(g), C.byref(ms)) != 0:
+                return out
+            out.append((b.value, g.value, ms.value))
+            i += 1
+
+    def chosen(self) -> tuple[int, int]:
+        b, g = C.c_uint32(), C.c_uint32()
+        N.check(N.lib().ion_batch_tuning(self._h, 0xFFFFFFFF, C.byref(b), C.byref(g), None))
+        return b.value, g.value
+
+    def record_event(self, slot: int) -> None:
+        N.check(N.lib().ion_batch_record_event(self._h, slot))
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        ms = C.c_float()
+        N.check(N.lib().ion_batch_event_elapsed(self._h, a, b, C.byref(ms)))
+        return ms.value
+
+    def close(self) -> None:
+        if self._h:
+            N.lib().ion_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def taylor_green_fields(nx: int, ny: int, nz: int, periodicity: int = 1, amplitude: float = 0.25,
                         reference_density: bool = True):
     """Velocity (3 arrays) and density of src/setup.rs:458-543 in float32 (cell order n = x + (y + z ny) nx)."""

@@ -73,6 +73,30 @@ def mhd_box(n: int = 128, float_type: int = 2, depth: int = 4, field_mode: int =
     }
 
 
+def batch_domains(count: int = 96, float_type: int = 2, field_mode: int = 1, seed_sizes: int = 3,
+                  seed_magnets: int = 4) -> list[dict]:
+    """Uneven MHD domains: cube edges uniform from {32,48,64,80,96} (PCG64
+    seed 3); a disk magnet per domain with radius uniform in {4..12} cells,
+    thickness r/2, at a random centre that keeps it inside the walls (seed 4);
+    charge and velocity as in mhd_box with per-domain seeds 100+i / 200+i."""
+    edges = np.random.Generator(np.random.PCG64(seed_sizes)).choice([32, 48, 64, 80, 96], size=count)
+    rm = np.random.Generator(np.random.PCG64(seed_magnets))
+    cases = []
+    for i, n in enumerate(int(e) for e in edges):
+        r = float(rm.integers(4, 13))
+        t = max(2.0, r / 2.0)
+        lo_xy, hi_xy = r + 2.0, n - r - 2.0
+        lo_z, hi_z = t / 2 + 2.0, n - t / 2 - 2.0
+        c = (float(rm.uniform(lo_xy, hi_xy)), float(rm.uniform(lo_xy, hi_xy)), float(rm.uniform(lo_z, hi_z)))
+        case = mhd_box(n=n, float_type=float_type, field_mode=field_mode, magnet=False, seed_q=100 + i,
+                       seed_u=200 + i)
+        p0, p1, p2 = cylinder(c, r, t, axis=2)
+        case["meshes"] = [(p0, p1, p2, "magnet", (0.0, 0.0, MAGNETIZATION_SI))]
+        case["precompute_b"] = True
+        cases.append(case)
+    return cases
+
+
 MODEL_IDS = {"solid": 0, "magnet": 1, "charged": 2, "charged_ecr": 3}
 
 
