@@ -120,11 +120,29 @@ __device__ __forceinline__ void add_src(float rx, float ry, float rz, float4 val
     }
 }
 
+// FAST far field of one source: E += q R/|R|^3 and, for B, the two sums
+// A += qv/|R|^3 and W += (qv x p)/|R|^3, from which B = A x c - W at the end
+// (qv x (c - p) = qv x c - qv x p): 3 FMA per source instead of 9.
+// p = (px, py, pz, q), qv = (q vx, q vy, q vz, -), w = qv x p.
+__device__ __forceinline__ void far_fast(float cx, float cy, float cz, float4 p, float4 qv, float4 w, float* e, float* A,
+                                         float* W) {
+    const float rx = cx - p.x, ry = cy - p.y, rz = cz - p.z;
+    const float r2 = fmaf(rz, rz, fmaf(ry, ry, rx * rx));
+    float inv;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
+    const float inv3 = inv * inv * inv;
+    const float s = p.w * inv3;
+    e[0] = fmaf(s, rx, e[0]); e[1] = fmaf(s, ry, e[1]); e[2] = fmaf(s, rz, e[2]);
+    A[0] = fmaf(inv3, qv.x, A[0]); A[1] = fmaf(inv3, qv.y, A[1]); A[2] = fmaf(inv3, qv.z, A[2]);
+    W[0] = fmaf(inv3, w.x, W[0]); W[1] = fmaf(inv3, w.y, W[1]); W[2] = fmaf(inv3, w.z, W[2]);
+}
+
 // Shared-memory staging area of one thread block; the mbarrier phase of each
 // buffer is tracked in `uses` so one block can process many tiles.
 struct EbSmem {
     float4 pos[2][SRC_CHUNK];
     float4 val[2][SRC_CHUNK];
+    float4 wv[2][SRC_CHUNK];  // FAST: qv x p of each source
     uint64_t bar[2];
 };
 
@@ -147,6 +165,7 @@ template <bool FAST>
 __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t tile, EbSmem& sm, uint32_t (&uses)[2]) {
     const uint32_t N = L.n;
     float fx[EB_CPT], fy[EB_CPT], fz[EB_CPT], e[EB_CPT][3], b[EB_CPT][3];
+    float Af[EB_CPT][3], Wf[EB_CPT][3];  // FAST far-field sums of the split cross product
     uint32_t own[EB_CPT];
     bool active[EB_CPT];
 #pragma unroll
@@ -159,7 +178,7 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t tile, Eb
         own[k] = n < N ? x / L.bsx + (y / L.bsy + z / L.bsz * L.nd) * L.nd : 0xFFFFFFFFu;
         if (!active[k]) own[k] = 0xFFFFFFFFu;
 #pragma unroll
-        for (int c = 0; c < 3; c++) { e[k][c] = 0.0f; b[k][c] = 0.0f; }
+        for (int c = 0; c < 3; c++) { e[k][c] = 0.0f; b[k][c] = 0.0f; Af[k][c] = 0.0f; Wf[k][c] = 0.0f; }
         // near field: the cell's aligned block (sim_kernels.cl:907-938)
         if (active[k]) {
             const uint32_t x0 = (x / L.near_x) * L.near_x, y0 = (y / L.near_y) * L.near_y, z0 = (z / L.near_z) * L.near_z;
@@ -202,10 +221,13 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t tile, Eb
         uses[buf]++;
         const uint32_t base = first + c * SRC_CHUNK;
         const uint32_t cnt = min(SRC_CHUNK, last - base);
-        if constexpr (FAST) {  // fold the charge into the velocity once per tile
+        if constexpr (FAST) {  // per source: (p, q), q v and q v x p, once per tile
             for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
-                const float4 v = sm.val[buf][k];
-                sm.val[buf][k] = make_float4(v.x, v.x * v.y, v.x * v.z, v.x * v.w);
+                const float4 p = sm.pos[buf][k], v = sm.val[buf][k];
+                const float qx = v.x * v.y, qy = v.x * v.z, qz = v.x * v.w;
+                sm.pos[buf][k] = make_float4(p.x, p.y, p.z, v.x);
+                sm.val[buf][k] = make_float4(qx, qy, qz, 0.0f);
+                sm.wv[buf][k] = make_float4(qy * p.z - qz * p.y, qz * p.x - qx * p.z, qx * p.y - qy * p.x, 0.0f);
             }
             __syncthreads();
         }
@@ -214,19 +236,34 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t tile, Eb
         for (uint32_t k = 0; k < EB_CPT; k++) here |= (own[k] - base) < cnt;
         const float4* sp = &sm.pos[buf][0];
         const float4* sv = &sm.val[buf][0];
+        const float4* sw = &sm.wv[buf][0];
         if (__any_sync(0xFFFFFFFFu, here)) {  // this chunk holds some cell's own bin
             for (uint32_t s = 0; s < cnt; s++) {
                 const float4 p = sp[s], v = sv[s];
+                if constexpr (FAST) {
+                    const float4 w = sw[s];
 #pragma unroll
-                for (uint32_t k = 0; k < EB_CPT; k++)
-                    if (base + s != own[k]) add_src<FAST>(fx[k] - p.x, fy[k] - p.y, fz[k] - p.z, v, e[k], b[k]);
+                    for (uint32_t k = 0; k < EB_CPT; k++)
+                        if (base + s != own[k]) far_fast(fx[k], fy[k], fz[k], p, v, w, e[k], Af[k], Wf[k]);
+                } else {
+#pragma unroll
+                    for (uint32_t k = 0; k < EB_CPT; k++)
+                        if (base + s != own[k]) add_src<false>(fx[k] - p.x, fy[k] - p.y, fz[k] - p.z, v, e[k], b[k]);
+                }
             }
         } else {
 #pragma unroll 2
             for (uint32_t s = 0; s < cnt; s++) {
                 const float4 p = sp[s], v = sv[s];
+                if constexpr (FAST) {
+                    const float4 w = sw[s];
 #pragma unroll
-                for (uint32_t k = 0; k < EB_CPT; k++) add_src<FAST>(fx[k] - p.x, fy[k] - p.y, fz[k] - p.z, v, e[k], b[k]);
+                    for (uint32_t k = 0; k < EB_CPT; k++) far_fast(fx[k], fy[k], fz[k], p, v, w, e[k], Af[k], Wf[k]);
+                } else {
+#pragma unroll
+                    for (uint32_t k = 0; k < EB_CPT; k++)
+                        add_src<false>(fx[k] - p.x, fy[k] - p.y, fz[k] - p.z, v, e[k], b[k]);
+                }
             }
         }
         __syncthreads();  // everyone is done with this buffer before it is refilled
@@ -242,6 +279,11 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t tile, Eb
     for (uint32_t k = 0; k < EB_CPT; k++) {
         const uint32_t n = tile + threadIdx.x + k * blockDim.x;
         if (!active[k]) continue;
+        if constexpr (FAST) {  // B = near part + A x c - W
+            b[k][0] = b[k][0] + ((Af[k][1] * fz[k] - Af[k][2] * fy[k]) - Wf[k][0]);
+            b[k][1] = b[k][1] + ((Af[k][2] * fx[k] - Af[k][0] * fz[k]) - Wf[k][1]);
+            b[k][2] = b[k][2] + ((Af[k][0] * fy[k] - Af[k][1] * fx[k]) - Wf[k][2]);
+        }
         L.e_dyn[n] = L.e_stat[n] + L.ke * e[k][0];
         L.e_dyn[(size_t)N + n] = L.e_stat[(size_t)N + n] + L.ke * e[k][1];
         L.e_dyn[2 * (size_t)N + n] = L.e_stat[2 * (size_t)N + n] + L.ke * e[k][2];

@@ -51,6 +51,15 @@ int fail(int code, const char* fmt, ...) {
                                            __FILE__, __LINE__);                                       \
     } while (0)
 
+}  // namespace
+
+namespace ion {
+int api_fail(int code, const char* message) { return fail(code, "%s", message); }
+void api_count_launches(uint64_t n) { g_launches += n; }
+}  // namespace ion
+
+namespace {
+
 // ---------------------------------------------------------------------------
 // Units -> kernel constants (src/lbm/units.rs:259-307; domain.rs:808, 839, 848),
 // evaluated in the same f32/f64 steps as the Rust code.

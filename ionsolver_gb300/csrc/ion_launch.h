@@ -27,7 +27,7 @@ constexpr unsigned RED_BLOCK = 256;
 
 // Cells per thread of the E/B update: each staged source is applied to
 // EB_CPT cells held in registers (cells tile + threadIdx.x + k*blockDim.x).
-constexpr uint32_t EB_CPT = 2;
+constexpr uint32_t EB_CPT = 4;
 
 // device view of a batch of domains (batch_kernels.cu)
 struct BatchDev {
@@ -66,4 +66,10 @@ void launch_fma_probe(float* out, int blocks, int iters, cudaStream_t s);
 void launch_codec(int ft, const float* in, uint16_t* enc, float* dec, const uint16_t* raw, float* raw_dec, uint64_t n,
                   cudaStream_t s);
 
+}  // namespace ion
+
+namespace ion {
+// error reporting and launch accounting of the C ABI (ion_api.cu)
+int api_fail(int code, const char* message);
+void api_count_launches(uint64_t n);
 }  // namespace ion
