@@ -238,6 +238,37 @@ int ion_lbm_set_kernel_timing(ion_lbm* h, int enable);
 int ion_lbm_kernel_time(ion_lbm* h, int kernel, double* total_ms, uint64_t* launches);
 int ion_lbm_reset_kernel_time(ion_lbm* h);
 
+/* ---- learned far field (no reference counterpart; it stands in for the far
+ *      part of update_e_b_dynamic, src/kernels/sim_kernels.cl:940-955).
+ *      Per cell, LOD bins within Chebyshev distance 2 of the cell's own bin
+ *      are summed exactly; the rest comes from a linear 3-D convolutional
+ *      network on the LOD grid (4 channels in: q, q*v; 48 out: E and B at the
+ *      8 corner cells of every block), interpolated trilinearly.  Every step a
+ *      sampled-cell check against the exact sum decides on the device whether
+ *      the exact kernel recomputes the field.  Needs ext_magneto_hydro, LOD
+ *      depth >= 2 and an empty reference near field. -------------------- */
+/* Generates `samples` snapshots (random charge and current per bin, exact
+ * far-field targets), trains with Adam on the GPU; rel_err = held-out
+ * relative L2 error of the BF16 inference path. */
+int ion_lbm_surrogate_train(ion_lbm* h, uint32_t samples, uint32_t epochs, uint32_t batch, float lr, uint64_t seed,
+                            float* rel_err);
+int ion_lbm_surrogate_info(ion_lbm* h, float* rel_err_fp32, float* rel_err_bf16, float* loss, uint32_t loss_cap,
+                           uint32_t* epochs);
+int ion_lbm_surrogate_save(ion_lbm* h, const char* path);
+int ion_lbm_surrogate_load(ion_lbm* h, const char* path);
+/* relative tolerance of the sampled check (default 1e-2) and cells per check (default 1024) */
+int ion_lbm_surrogate_configure(ion_lbm* h, float tolerance, uint32_t check_cells);
+/* checks run, fallbacks taken, last relative errors of E and B */
+int ion_lbm_surrogate_stats(ion_lbm* h, uint64_t* checks, uint64_t* fallbacks, float* err_e, float* err_b);
+/* network weights (get into `out` and/or set from `in`; count = number of weights) */
+int ion_lbm_surrogate_weights(ion_lbm* h, float* out, const float* in, size_t count);
+/* loss and weight gradient of one batch: x [batch][4][V], t [batch][48][V] (host) */
+int ion_lbm_surrogate_grad(ion_lbm* h, const float* x, const float* t, uint32_t batch, float* loss, float* grad);
+/* one forward pass of x [4][V] into y [48][V] (host); bf16 != 0: tensor-core path */
+int ion_lbm_surrogate_forward(ion_lbm* h, const float* x, float* y, int bf16);
+/* switches the field mode of an MHD handle (ION_FIELD_*) */
+int ion_lbm_set_field_mode(ion_lbm* h, int mode);
+
 /* ---- batches of independent domains (no reference counterpart; the
  *      reference advances one domain per OpenCL queue, src/lbm/mod.rs:250-272)
  *      Every domain of a batch keeps its own buffers, size, units and flags;

@@ -93,6 +93,19 @@ _SIGS = {
     "ion_lbm_kernel_time": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
     "ion_lbm_reset_kernel_time": (C.c_int, [_P]),
     "ion_codec_roundtrip": (C.c_int, [C.c_int, _P, _P, _P, _P, _P, C.c_uint64]),
+    "ion_lbm_surrogate_train": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, C.c_uint64,
+                                          C.POINTER(C.c_float)]),
+    "ion_lbm_surrogate_info": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                         C.c_uint32, C.POINTER(C.c_uint32)]),
+    "ion_lbm_surrogate_save": (C.c_int, [_P, C.c_char_p]),
+    "ion_lbm_surrogate_load": (C.c_int, [_P, C.c_char_p]),
+    "ion_lbm_surrogate_configure": (C.c_int, [_P, C.c_float, C.c_uint32]),
+    "ion_lbm_surrogate_stats": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_float),
+                                          C.POINTER(C.c_float)]),
+    "ion_lbm_surrogate_weights": (C.c_int, [_P, _P, _P, C.c_size_t]),
+    "ion_lbm_surrogate_grad": (C.c_int, [_P, _P, _P, C.c_uint32, C.POINTER(C.c_float), _P]),
+    "ion_lbm_surrogate_forward": (C.c_int, [_P, _P, _P, C.c_int]),
+    "ion_lbm_set_field_mode": (C.c_int, [_P, C.c_int]),
     "ion_batch_create": (C.c_int, [C.POINTER(_P), C.c_uint32, C.POINTER(_P)]),
     "ion_batch_destroy": (C.c_int, [_P]),
     "ion_batch_run": (C.c_int, [_P, C.c_uint64]),

@@ -8,6 +8,10 @@ void launch_lod_bins(const DevLbm& L, cudaStream_t s) {
     k_lod_bins<<<grid_for(threads, 256), 256, 0, s>>>(L);
 }
 
+void launch_update_e_b_gated(const DevLbm& L, uint32_t* err, const uint32_t* gate, cudaStream_t s) {
+    k_update_e_b_gated<<<grid_for(L.n, 256 * EB_CPT), 256, 0, s>>>(L, err, gate);
+}
+
 void launch_update_e_b(const DevLbm& L, bool fast, uint32_t* err, cudaStream_t s) {
     const unsigned g = grid_for(L.n, 256 * EB_CPT);
     if (fast) k_update_e_b<true><<<g, 256, 0, s>>>(L, err);

@@ -294,6 +294,15 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t tile, Eb
     return true;
 }
 
+// The exact update, run only when *gate != 0 (the surrogate's fallback decision)
+static __global__ void __launch_bounds__(256) k_update_e_b_gated(const DevLbm L, uint32_t* err, const uint32_t* gate) {
+    if (*gate == 0u) return;
+    __shared__ __align__(16) EbSmem sm;
+    eb_init(sm);
+    uint32_t uses[2] = {0u, 0u};
+    if (!eb_tile<true>(L, blockIdx.x * blockDim.x * EB_CPT, sm, uses) && threadIdx.x == 0) atomicExch(err, 1u);
+}
+
 template <bool FAST>
 static __global__ void __launch_bounds__(256) k_update_e_b(const DevLbm L, uint32_t* err) {
     __shared__ __align__(16) EbSmem sm;

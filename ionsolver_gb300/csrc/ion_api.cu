@@ -17,8 +17,11 @@
 #include <thread>
 #include <vector>
 
+#include <memory>
+
 #include "ion_device.cuh"
 #include "ion_launch.h"
+#include "surrogate.h"
 
 using namespace ion;
 
@@ -117,8 +120,14 @@ int validate(const ion_config& c) {
         const uint32_t nd = 1u << c.mhd_lod_depth;
         if (c.n_x % nd || c.n_y % nd || c.n_z % nd)
             return fail(ION_E_CONFIG, "with ext_magneto_hydro, n_x/n_y/n_z must be multiples of 2^mhd_lod_depth");
-        if (c.field_mode != ION_FIELD_BITWISE && c.field_mode != ION_FIELD_FAST)
+        if (c.field_mode > ION_FIELD_SURROGATE)
             return fail(ION_E_CONFIG, "field_mode %d is not available", (int)c.field_mode);
+        if (c.field_mode == ION_FIELD_SURROGATE) {
+            const uint32_t big = 1u << (1u << c.mhd_lod_depth);
+            if (c.mhd_lod_depth < 2 || c.n_x / big > 1 || c.n_y / big > 1 || c.n_z / big > 1)
+                return fail(ION_E_CONFIG, "the learned far field needs LOD depth >= 2 and an empty reference near field "
+                                          "(n/2^(2^D) <= 1 on every axis)");
+        }
     }
     if (c.ext_force_field && !c.ext_volume_force) return fail(ION_E_CONFIG, "ext_force_field needs ext_volume_force");
     return ION_OK;
@@ -174,6 +183,7 @@ struct ion_lbm {
     std::vector<HostMesh> meshes;
     cudaGraphExec_t graph = nullptr;
     uint32_t graph_kernels = 0;
+    bool graph_dirty = false;  // the step's launch sequence changed since capture
     cudaEvent_t ev[8] = {};
     bool ktiming = false;
     std::vector<KEv> kev;
@@ -181,6 +191,7 @@ struct ion_lbm {
     double ktime[3] = {0, 0, 0};
     uint64_t kcount[3] = {0, 0, 0};
     std::vector<void*> allocs;
+    std::unique_ptr<ion::Surrogate> sur;  // learned far field (field_mode SURROGATE)
 };
 
 namespace {
@@ -224,8 +235,20 @@ int launch_stream_collide(ion_lbm* h, uint64_t t) {
 }
 
 int launch_field(ion_lbm* h) {
-    launch_update_e_b(h->L, h->cfg.field_mode == ION_FIELD_FAST, h->d_err, h->stream);
+    // the exact sum; SURROGATE handles use its FAST arithmetic outside the surrogate path
+    launch_update_e_b(h->L, h->cfg.field_mode != ION_FIELD_BITWISE, h->d_err, h->stream);
     g_launches++;
+    CKL();
+    return ION_OK;
+}
+
+// learned far field + sampled exact check + device-decided exact fallback
+int launch_surrogate_field(ion_lbm* h) {
+    if (!h->sur || !h->sur->ready())
+        return fail(ION_E_STATE, "field_mode SURROGATE: train (ion_lbm_surrogate_train) or load the network first");
+    h->sur->step(h->L, h->stream, 0x2545F491u);
+    launch_update_e_b_gated(h->L, h->d_err, h->sur->fallback_flag(), h->stream);
+    g_launches += h->sur->launches_per_step() + 1;
     CKL();
     return ION_OK;
 }
@@ -266,14 +289,18 @@ int enqueue_step(ion_lbm* h, uint64_t t) {
     if (h->cfg.ext_magneto_hydro) {
         rc = timed(h, 2, [&] { return launch_bins(h); });
         if (rc) return rc;
-        rc = timed(h, 1, [&] { return launch_field(h); });
+        rc = timed(h, 1, [&] {
+            return h->cfg.field_mode == ION_FIELD_SURROGATE ? launch_surrogate_field(h) : launch_field(h);
+        });
         if (rc) return rc;
     }
     return ION_OK;
 }
 
 uint32_t kernels_per_step(const ion_lbm* h) {
-    return 1u + (h->cfg.ext_magneto_hydro ? (h->L.depth > 0 ? 2u : 1u) : 0u);
+    uint32_t k = 1u + (h->cfg.ext_magneto_hydro ? (h->L.depth > 0 ? 2u : 1u) : 0u);
+    if (h->cfg.ext_magneto_hydro && h->cfg.field_mode == ION_FIELD_SURROGATE && h->sur) k += h->sur->launches_per_step();
+    return k;
 }
 
 int check_device_error(ion_lbm* h) {
@@ -579,6 +606,11 @@ int ion_lbm_run(ion_lbm* h, uint64_t steps) {
         if (rc) return rc;
         steps--;
     }
+    if (h->graph && h->graph_dirty) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    h->graph_dirty = false;
     if (!h->graph) {
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -1262,6 +1294,127 @@ int ion_batch_event_elapsed(ion_batch* b, int a, int c, float* ms) {
     if (!b || !ms || a < 0 || a >= 4 || c < 0 || c >= 4) return fail(ION_E_INVALID, "bad event slot");
     CK(cudaEventSynchronize(b->ev[c]));
     CK(cudaEventElapsedTime(ms, b->ev[a], b->ev[c]));
+    return ION_OK;
+}
+
+// ---- learned far field ------------------------------------------------------------
+static int ensure_surrogate(ion_lbm* h) {
+    if (!h->cfg.ext_magneto_hydro) return fail(ION_E_STATE, "the learned far field needs ext_magneto_hydro");
+    const uint32_t big = 1u << h->L.nd;
+    if (h->L.depth < 2 || h->L.nx / big > 1 || h->L.ny / big > 1 || h->L.nz / big > 1)
+        return fail(ION_E_CONFIG, "the learned far field needs LOD depth >= 2 and an empty reference near field");
+    if (h->sur) return ION_OK;
+    h->sur.reset(new ion::Surrogate());
+    const int rc = h->sur->init((int)h->L.nd, (float)h->L.bsx, (float)h->L.bsy, (float)h->L.bsz, (int)h->L.first_src);
+    if (rc) { h->sur.reset(); return fail(rc, "surrogate buffers"); }
+    return ION_OK;
+}
+
+int ion_lbm_surrogate_train(ion_lbm* h, uint32_t samples, uint32_t epochs, uint32_t batch, float lr, uint64_t seed,
+                            float* rel_err) {
+    if (!h) return fail(ION_E_INVALID, "null handle");
+    if (samples < 2 || batch == 0 || batch > samples) return fail(ION_E_INVALID, "bad sample/batch counts");
+    int rc = ensure_surrogate(h);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->stream));
+    rc = h->sur->train((int)samples, (int)epochs, (int)batch, lr, seed, h->stream, rel_err);
+    if (rc) return fail(rc, "surrogate training failed");
+    h->graph_dirty = true;
+    return ION_OK;
+}
+
+int ion_lbm_surrogate_info(ion_lbm* h, float* rel_err_fp32, float* rel_err_bf16, float* loss, uint32_t loss_cap,
+                           uint32_t* epochs) {
+    if (!h || !h->sur) return fail(ION_E_STATE, "no surrogate");
+    if (rel_err_fp32) *rel_err_fp32 = h->sur->rel32();
+    if (rel_err_bf16) *rel_err_bf16 = h->sur->rel16();
+    const auto& L = h->sur->loss_history();
+    if (epochs) *epochs = (uint32_t)L.size();
+    for (uint32_t i = 0; loss && i < loss_cap && i < L.size(); i++) loss[i] = L[i];
+    return ION_OK;
+}
+
+int ion_lbm_surrogate_save(ion_lbm* h, const char* path) {
+    if (!h || !path) return fail(ION_E_INVALID, "null argument");
+    if (!h->sur || !h->sur->ready()) return fail(ION_E_STATE, "no trained surrogate");
+    const int rc = h->sur->save(path);
+    return rc ? fail(rc, "cannot write \"%s\"", path) : ION_OK;
+}
+
+int ion_lbm_surrogate_load(ion_lbm* h, const char* path) {
+    if (!h || !path) return fail(ION_E_INVALID, "null argument");
+    int rc = ensure_surrogate(h);
+    if (rc) return rc;
+    rc = h->sur->load(path, h->stream);
+    if (rc) return fail(rc, "cannot read a surrogate for this grid from \"%s\"", path);
+    h->graph_dirty = true;
+    return ION_OK;
+}
+
+int ion_lbm_surrogate_configure(ion_lbm* h, float tolerance, uint32_t check_cells) {
+    if (!h) return fail(ION_E_INVALID, "null handle");
+    int rc = ensure_surrogate(h);
+    if (rc) return rc;
+    if (!(tolerance >= 0.0f) || check_cells == 0) return fail(ION_E_INVALID, "bad tolerance or sample count");
+    h->sur->configure(tolerance, check_cells);
+    h->graph_dirty = true;
+    return ION_OK;
+}
+
+int ion_lbm_surrogate_stats(ion_lbm* h, uint64_t* checks, uint64_t* fallbacks, float* err_e, float* err_b) {
+    if (!h || !h->sur) return fail(ION_E_STATE, "no surrogate");
+    unsigned long long* c;
+    float* last;
+    h->sur->stats_device(&c, &last);
+    unsigned long long hc[2] = {0, 0};
+    float hl[2] = {0, 0};
+    CK(cudaMemcpyAsync(hc, c, sizeof hc, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(hl, last, sizeof hl, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (checks) *checks = hc[0];
+    if (fallbacks) *fallbacks = hc[1];
+    if (err_e) *err_e = hl[0];
+    if (err_b) *err_b = hl[1];
+    return ION_OK;
+}
+
+int ion_lbm_surrogate_weights(ion_lbm* h, float* out, const float* in, size_t count) {
+    if (!h) return fail(ION_E_INVALID, "null handle");
+    int rc = ensure_surrogate(h);
+    if (rc) return rc;
+    if (count != h->sur->weight_count())
+        return fail(ION_E_INVALID, "the network has %zu weights, got %zu", h->sur->weight_count(), count);
+    if (out) { rc = h->sur->get_weights(out); if (rc) return fail(rc, "weights"); }
+    if (in) { rc = h->sur->set_weights(in, h->stream); if (rc) return fail(rc, "weights"); h->graph_dirty = true; }
+    return ION_OK;
+}
+
+int ion_lbm_surrogate_grad(ion_lbm* h, const float* x, const float* t, uint32_t batch, float* loss, float* grad) {
+    if (!h || !x || !t || !loss || !grad || batch == 0) return fail(ION_E_INVALID, "null argument");
+    int rc = ensure_surrogate(h);
+    if (rc) return rc;
+    rc = h->sur->grad(x, t, (int)batch, loss, grad, h->stream);
+    return rc ? fail(rc, "surrogate gradient") : ION_OK;
+}
+
+int ion_lbm_surrogate_forward(ion_lbm* h, const float* x, float* y, int bf16) {
+    if (!h || !x || !y) return fail(ION_E_INVALID, "null argument");
+    int rc = ensure_surrogate(h);
+    if (rc) return rc;
+    rc = h->sur->forward(x, y, bf16 != 0, h->stream);
+    return rc ? fail(rc, "surrogate forward") : ION_OK;
+}
+
+int ion_lbm_set_field_mode(ion_lbm* h, int mode) {
+    if (!h) return fail(ION_E_INVALID, "null handle");
+    if (!h->cfg.ext_magneto_hydro) return fail(ION_E_STATE, "field modes apply to ext_magneto_hydro");
+    if (mode < ION_FIELD_BITWISE || mode > ION_FIELD_SURROGATE) return fail(ION_E_INVALID, "unknown field mode %d", mode);
+    if (mode == ION_FIELD_SURROGATE) {
+        int rc = ensure_surrogate(h);
+        if (rc) return rc;
+    }
+    h->cfg.field_mode = (uint8_t)mode;
+    h->graph_dirty = true;
     return ION_OK;
 }
 

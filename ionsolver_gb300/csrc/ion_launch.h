@@ -56,6 +56,7 @@ ION_DECLARE_LBM_DISPATCH(q9)
 
 void launch_lod_bins(const DevLbm& L, cudaStream_t s);
 void launch_update_e_b(const DevLbm& L, bool fast, uint32_t* err, cudaStream_t s);
+void launch_update_e_b_gated(const DevLbm& L, uint32_t* err, const uint32_t* gate, cudaStream_t s);
 void launch_voxelize(const DevLbm& L, const VoxArgs& A, cudaStream_t s);
 void launch_compact(const DevLbm& L, uint8_t mask, uint32_t* tiles, uint32_t* list, uint32_t* total, cudaStream_t s);
 void launch_psi_static_b(const DevLbm& L, const uint32_t* mags, const uint32_t* count, cudaStream_t s);

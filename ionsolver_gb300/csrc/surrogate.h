@@ -1,0 +1,73 @@
+// surrogate.h -- the learned far field of the E/B update (surrogate.cu).
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "ion_device.cuh"
+
+namespace ion {
+
+class Surrogate {
+public:
+    static constexpr int RNEAR = 2;  // bins within this Chebyshev distance are summed exactly
+    ~Surrogate();
+    int init(int nd, float bsx, float bsy, float bsz, int first_src);
+    // generates `nsamples` snapshots (random charge/current per bin, exact far-field
+    // targets), trains with Adam, returns the held-out relative L2 error of the BF16 path
+    int train(int nsamples, int epochs, int batch, float lr, uint64_t seed, cudaStream_t s, float* rel_err);
+    int save(const char* path) const;
+    int load(const char* path, cudaStream_t s);
+    // one step: source scales, network input, BF16 inference, per-cell field,
+    // sampled exact check and the fallback decision (device flag)
+    void step(const DevLbm& L, cudaStream_t s, uint32_t salt);
+    uint32_t launches_per_step() const;
+    bool ready() const { return ready_; }
+    const uint32_t* fallback_flag() const { return flag_; }
+    void configure(float tol, uint32_t cells) { tol_ = tol; check_cells_ = cells; }
+    float tol() const { return tol_; }
+    uint32_t check_cells() const { return check_cells_; }
+    // [0] checks, [1] fallbacks (device counters), [2..3] last relative errors
+    void stats_device(unsigned long long** counters, float** last) { *counters = counters_; *last = last_; }
+    float rel32() const { return rel32_; }
+    float rel16() const { return rel16_; }
+    const std::vector<float>& loss_history() const { return loss_; }
+    void infer_bf16(const float* X, cudaStream_t s);
+    size_t weight_count() const { return nw_; }
+    int get_weights(float* host) const;
+    int set_weights(const float* host, cudaStream_t s);
+    // loss and weight gradient of one batch (host arrays; targets in the network's output scale)
+    int grad(const float* hX, const float* hT, int B, float* loss, float* hgrad, cudaStream_t s);
+    // FP32 (bf16=false) or BF16 tensor-core (bf16=true) forward of one sample (host arrays)
+    int forward(const float* hX, float* hY, bool bf16, cudaStream_t s);
+
+private:
+    int alloc(void** p, size_t bytes);
+    void forward_fp32(const float* X, int B, std::vector<float*>& acts, float* Y, cudaStream_t s);
+    void backward_fp32(const float* X, int B, std::vector<float*>& acts, const float* gY, std::vector<float*>& g,
+                       cudaStream_t s);
+    void pack_bf16(cudaStream_t s);
+    void k_pack_input_dev(const DevLbm& L, cudaStream_t s);
+
+    int nd_ = 0, V_ = 0, first_ = 0;
+    float bs_[3] = {1, 1, 1};
+    size_t woff_[10] = {};
+    size_t nw_ = 0;
+    float *w_ = nullptr, *gw_ = nullptr, *m_ = nullptr, *v_ = nullptr, *wt_ = nullptr;
+    __nv_bfloat16* wk_ = nullptr;
+    float *scales_ = nullptr, *last_ = nullptr, *xin_ = nullptr, *yout_ = nullptr, *ha_ = nullptr, *hb_ = nullptr;
+    __nv_bfloat16 *ab_ = nullptr, *bb_ = nullptr;
+    uint32_t *stats_ = nullptr, *flag_ = nullptr;
+    unsigned long long* counters_ = nullptr;
+    float yE_ = 1.0f, yB_ = 1.0f;
+    float tol_ = 1e-2f;
+    uint32_t check_cells_ = 1024;
+    float rel32_ = -1.0f, rel16_ = -1.0f;
+    bool ready_ = false;
+    std::vector<float> loss_;
+    std::vector<void*> allocs_;
+};
+
+}  // namespace ion

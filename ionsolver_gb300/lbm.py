@@ -335,6 +335,64 @@ class Lbm:
         N.check(N.lib().ion_lbm_load(str(path).encode(), C.byref(c), C.byref(h)))
         return Lbm(_handle=h)
 
+    # -- learned far field ----------------------------------------------------------------
+    def surrogate_train(self, samples: int = 2000, epochs: int = 20, batch: int = 8, lr: float = 1e-3,
+                        seed: int = 5) -> float:
+        err = C.c_float()
+        N.check(N.lib().ion_lbm_surrogate_train(self._h, samples, epochs, batch, lr, seed, C.byref(err)))
+        return err.value
+
+    def surrogate_info(self) -> dict:
+        r32, r16, n = C.c_float(), C.c_float(), C.c_uint32()
+        loss = (C.c_float * 1024)()
+        N.check(N.lib().ion_lbm_surrogate_info(self._h, C.byref(r32), C.byref(r16), loss, 1024, C.byref(n)))
+        return {"rel_err_fp32": r32.value, "rel_err_bf16": r16.value, "loss": list(loss)[: n.value]}
+
+    def surrogate_save(self, path: str) -> None:
+        N.check(N.lib().ion_lbm_surrogate_save(self._h, str(path).encode()))
+
+    def surrogate_load(self, path: str) -> None:
+        N.check(N.lib().ion_lbm_surrogate_load(self._h, str(path).encode()))
+
+    def surrogate_configure(self, tolerance: float = 1e-2, check_cells: int = 1024) -> None:
+        N.check(N.lib().ion_lbm_surrogate_configure(self._h, tolerance, check_cells))
+
+    def surrogate_stats(self) -> dict:
+        c, f, e, b = C.c_uint64(), C.c_uint64(), C.c_float(), C.c_float()
+        N.check(N.lib().ion_lbm_surrogate_stats(self._h, C.byref(c), C.byref(f), C.byref(e), C.byref(b)))
+        return {"checks": c.value, "fallbacks": f.value, "err_e": e.value, "err_b": b.value}
+
+    def surrogate_weights(self, values=None) -> np.ndarray:
+        n = self._surrogate_count()
+        out = np.empty(n, np.float32)
+        src = None if values is None else np.ascontiguousarray(values, np.float32)
+        N.check(N.lib().ion_lbm_surrogate_weights(self._h, out.ctypes.data, None if src is None else src.ctypes.data, n))
+        return out
+
+    def _surrogate_count(self) -> int:
+        # layer table of the network (4->32, 8 x 32->32, 32->48; 3^3 kernels)
+        return (4 * 32 + 8 * 32 * 32 + 32 * 48) * 27
+
+    def surrogate_grad(self, x: np.ndarray, t: np.ndarray) -> tuple[float, np.ndarray]:
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        g = np.empty(self._surrogate_count(), np.float32)
+        loss = C.c_float()
+        N.check(N.lib().ion_lbm_surrogate_grad(self._h, x.ctypes.data, t.ctypes.data, x.shape[0], C.byref(loss),
+                                               g.ctypes.data))
+        return loss.value, g
+
+    def surrogate_forward(self, x: np.ndarray, bf16: bool = False) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.float32).reshape(-1)
+        V = x.size // 4
+        y = np.empty(48 * V, np.float32)
+        N.check(N.lib().ion_lbm_surrogate_forward(self._h, x.ctypes.data, y.ctypes.data, int(bf16)))
+        return y
+
+    def set_field_mode(self, mode: int) -> None:
+        N.check(N.lib().ion_lbm_set_field_mode(self._h, int(mode)))
+        self.config.field_mode = int(mode)
+
     # -- timing ---------------------------------------------------------------------------
     def record_event(self, slot: int) -> None:
         N.check(N.lib().ion_lbm_record_event(self._h, slot))
