@@ -290,6 +290,23 @@ int ion_batch_tuning(ion_batch* b, uint32_t i, uint32_t* block, uint32_t* grid, 
 int ion_batch_record_event(ion_batch* b, int slot);
 int ion_batch_event_elapsed(ion_batch* b, int start, int end, float* ms);
 
+/* ---- FP64 sum without device allocation (no counterpart in the reference) --
+ * Sum, in double precision, of `count` stored DDF values (decoded with
+ * float_type) at device address d_values; the result is written to the
+ * device double *d_sum, ordered on `stream` (a cudaStream_t, 0 = default).
+ * For callers that cannot call cudaMalloc/cudaFree where they need the sum:
+ * a host whose device memory is fully reserved by its own pool allocator, or
+ * a stepping loop that must not take the implicit synchronisation of
+ * cudaFree.  The scratch is a fixed 32 KiB array of partial sums in device
+ * memory, held by every GPU that loads this library until the process exits.
+ * At most ION_NOALLOC_MAX_VALUES values per call (else ION_E_INVALID).  The
+ * first call on a device looks the array up with that device current; make
+ * it before any stream capture.  All calls on a device share the array, so
+ * calls that overlap on the GPU race; each call rewrites every partial it
+ * reads, so nothing needs clearing between calls. */
+#define ION_NOALLOC_MAX_VALUES 268435456ull
+int ion_ddf_sum_f64_noalloc(const void* d_values, int float_type, uint64_t count, double* d_sum, void* stream);
+
 /* ---- storage codecs on the device (no reference counterpart; exposes the
  *      FP16S/FP16C codecs of src/lbm/domain.rs:773-780 and
  *      src/kernels/sim_kernels.cl:79-90 for exhaustive checks) ------------ */

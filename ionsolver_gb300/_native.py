@@ -93,6 +93,7 @@ _SIGS = {
     "ion_lbm_kernel_time": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
     "ion_lbm_reset_kernel_time": (C.c_int, [_P]),
     "ion_codec_roundtrip": (C.c_int, [C.c_int, _P, _P, _P, _P, _P, C.c_uint64]),
+    "ion_ddf_sum_f64_noalloc": (C.c_int, [_P, C.c_int, C.c_uint64, _P, _P]),
     "ion_lbm_surrogate_train": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, C.c_uint64,
                                           C.POINTER(C.c_float)]),
     "ion_lbm_surrogate_info": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
