@@ -10,6 +10,12 @@ Workloads (``--workload``; default ``mhd128``, the headline configuration):
   batch96 : 96 independent MHD domains, cube edges from {32,48,64,80,96}
       (seed 3), a disk magnet each (radius 4..12, seed 4), one persistent
       launch per step for all of them, autotuned launch shape, CUDA graph.
+  rings384 : 384^3, FP16S storage, two coaxial ring magnets (R_out 48, R_in 32,
+      t 12, centres 128 apart, axis z; rings192 the same at half scale, for
+      profiling), LOD depth 4, the learned far field
+      (network trained before the timed region on 2000 exact snapshots, seed
+      5) with the sampled exact check and device-decided exact fallback; the
+      line also carries the exact FP32 step of the same box for comparison.
   tgv64/256/384 : plain D3Q19 SRT FP32, periodic Taylor-Green vortex (u0 0.05).
 A step is one timestep of every cell (stream_collide, LOD bins, E/B update).
 Metric: MLUPs/s = cells * steps / seconds / 1e6.
@@ -63,25 +69,39 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="mhd128",
-                   choices=["mhd128", "mhd256", "mhd64", "batch96", "tgv64", "tgv256", "tgv384"])
-    p.add_argument("--field-mode", default="fast", choices=["bitwise", "fast"])
-    p.add_argument("--float-type", default="FP32", choices=["FP32", "FP16S", "FP16C"])
+                   choices=["mhd128", "mhd256", "mhd64", "batch96", "rings384", "rings192", "tgv64", "tgv256",
+                            "tgv384"])
+    p.add_argument("--field-mode", default=None, choices=["bitwise", "fast", "surrogate"],
+                   help="default: surrogate for rings384, fast otherwise")
+    p.add_argument("--float-type", default=None, choices=["FP32", "FP16S", "FP16C"],
+                   help="default: FP16S for rings384, FP32 otherwise")
+    p.add_argument("--train-samples", type=int, default=2000, help="rings384: exact snapshots to train on")
+    p.add_argument("--train-epochs", type=int, default=20)
     p.add_argument("--ref-seconds", type=float, default=20.0, help="CPU time budget of the reference/baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    return p.parse_args()
+    a = p.parse_args()
+    rings = a.workload.startswith("rings")
+    a.field_mode = a.field_mode or ("surrogate" if rings else "fast")
+    a.float_type = a.float_type or ("FP16S" if rings else "FP32")
+    if a.field_mode == "surrogate" and not rings:
+        p.error("--field-mode surrogate needs --workload rings384 or rings192")
+    return a
 
 
 FT = {"FP16S": 0, "FP16C": 1, "FP32": 2}
+FM = {"bitwise": 0, "fast": 1, "surrogate": 2}
 
 
 def make_cases(a) -> list[dict]:
     from ionsolver_gb300 import workloads as W
-    fm = 0 if a.field_mode == "bitwise" else 1
+    fm = FM[a.field_mode]
     ft = FT[a.float_type]
     w = a.workload
     if w == "batch96":
         return W.batch_domains(96, float_type=ft, field_mode=fm)
+    if w.startswith("rings"):  # rings192: the same box at half the size (profiling case)
+        return [W.mhd_box(n=int(w[5:]), float_type=ft, depth=4, field_mode=fm, rings=True)]
     n = int(w[3:])
     if w.startswith("mhd"):
         return [W.mhd_box(n=n, float_type=ft, field_mode=fm, magnet_r=16.0 * n / 128, magnet_t=8.0 * n / 128)]
@@ -102,6 +122,29 @@ def bytes_per_lup(cfg: dict) -> int:
         if cfg.get("mhd_lod_depth", 4) > 0:
             b += 12                          # velocity contribution to the LOD bins
     return b
+
+
+def near_interactions(cfg: dict, flags: np.ndarray, rnear: int = 2) -> int:
+    """Source terms the learned-far-field path sums exactly per step: fluid
+    cells x bins within Chebyshev distance rnear of their own bin (own bin
+    and bins below the source range excluded)."""
+    D = int(cfg["mhd_lod_depth"])
+    nd = 1 << D
+    n_own = 1 + sum(8 ** (i + 1) for i in range(D))
+    first = n_own - nd ** 3
+    nx, ny, nz = cfg["n_x"], cfg["n_y"], cfg["n_z"]
+    fl = ((flags & 0x1F) != 0x01).reshape(nd, nz // nd, nd, ny // nd, nd, nx // nd)
+    fluid_per_bin = fl.sum(axis=(1, 3, 5))  # [bz][by][bx]
+    idx = np.arange(nd ** 3).reshape(nd, nd, nd)
+    total = 0
+    for bz in range(nd):
+        for by in range(nd):
+            for bx in range(nd):
+                sl = idx[max(bz - rnear, 0):bz + rnear + 1, max(by - rnear, 0):by + rnear + 1,
+                         max(bx - rnear, 0):bx + rnear + 1]
+                own = bx + (by + bz * nd) * nd
+                total += int(fluid_per_bin[bz, by, bx]) * int(((sl >= first) & (sl != own)).sum())
+    return total
 
 
 def field_interactions(cfg: dict, flags: np.ndarray) -> int:
@@ -208,6 +251,17 @@ class Clocks:
                 "reasons": reasons, "samples": len(use), "window": "timed region" if inside else "whole run"}
 
 
+def cpu_sample_cases(a, cases: list[dict]) -> list[dict]:
+    """The host-core sample of a workload.  rings384: the same two-ring box at
+    96^3 -- at LOD depth 4 the reference's E/B update costs 4095 source terms
+    per cell at any box size, so its MLUPs/s carry over; a 384^3 step would
+    take minutes on the host cores."""
+    if a.workload.startswith("rings"):
+        from ionsolver_gb300 import workloads as W
+        return [W.mhd_box(n=96, float_type=FT[a.float_type], depth=4, field_mode=0, rings=True)]
+    return cases
+
+
 # ---------------------------------------------------------------------------
 def cpu_run(cases: list[dict], steps: int, budget_s: float, init_fields: list[dict] | None):
     """Advances the cases on the host cores within a time budget.
@@ -254,6 +308,77 @@ def cpu_run(cases: list[dict], steps: int, budget_s: float, init_fields: list[di
 
 
 # ---------------------------------------------------------------------------
+def _restart(lbm, case):
+    """The case's initial state again (initialize() reads rho, u, q and the LOD bins)."""
+    for n in ("rho", "u", "q"):
+        lbm.write(n, case["fields"][n])
+    lbm.write("qu_lod", np.zeros(lbm.field_info("qu_lod")[1], np.float32))
+    lbm.initialize()
+
+
+def _dyn(lbm, n):
+    """E_dyn and B_dyn, the fields the next step uses."""
+    return lbm.read("e_dyn")[:3 * n].astype(np.float64), lbm.read("b_dyn")[:3 * n].astype(np.float64)
+
+
+def _rel(x, ref):
+    return float(np.max(np.abs(x - ref)) / max(np.max(np.abs(ref)), 1e-300))
+
+
+def surrogate_setup(a, case: dict, lbm) -> dict:
+    """Trains the learned far field (untimed setup) and measures its field
+    error after the first step against the exact sum on the same state."""
+    t0 = time.perf_counter()
+    lbm.surrogate_train(samples=a.train_samples, epochs=a.train_epochs, batch=8, lr=2e-3, seed=5)
+    train_s = time.perf_counter() - t0
+    info = lbm.surrogate_info()
+    n = case["config"]["n_x"] * case["config"]["n_y"] * case["config"]["n_z"]
+    lbm.surrogate_configure(tolerance=1e30, check_cells=1024)
+    _restart(lbm, case)
+    lbm.do_time_step()
+    e_s, b_s = _dyn(lbm, n)
+    lbm.set_field_mode(1)
+    _restart(lbm, case)
+    lbm.do_time_step()
+    e_x, b_x = _dyn(lbm, n)
+    lbm.set_field_mode(2)
+    lbm.surrogate_configure(tolerance=1e-2, check_cells=1024)  # the run's settings; restarts the statistics
+    _restart(lbm, case)
+    return {"train_s": train_s, "train_samples": a.train_samples, "train_epochs": a.train_epochs, "seed": 5,
+            "rel_err_fp32_heldout": info["rel_err_fp32"], "rel_err_bf16_heldout": info["rel_err_bf16"],
+            "field_rel_err_step1": {"e": _rel(e_s, e_x), "b": _rel(b_s, b_x),
+                                    "against": "E_dyn, B_dyn of the exact FAST sum of the same state, "
+                                               "max|diff|/max|exact| (B_dyn is B_stat to float precision)"},
+            "loss_first_last": [info["loss"][0], info["loss"][-1]] if info["loss"] else None,
+            "check": {"tolerance": 1e-2, "cells": 1024}}
+
+
+def exact_fp32_step(case: dict, src) -> dict:
+    """The exact FP32 step (FAST field mode) of the same box, CUDA-event timed."""
+    import ionsolver_gb300 as I
+    from ionsolver_gb300 import workloads as W
+    cfg = dict(case["config"], float_type=2, field_mode=1)
+    ex = I.Lbm(W.lbm_config(dict(case, config=cfg)))
+    for n in ("flags", "b_stat"):
+        ex.write(n, src.read(n))
+    for n in ("rho", "u", "q"):
+        ex.write(n, case["fields"][n])
+    ex.initialize()
+    ex.do_time_step()
+    ex.finish_queues(600000)
+    steps = 2
+    ex.record_event(0)
+    for _ in range(steps):
+        ex.do_time_step()
+    ex.record_event(1)
+    ms = ex.elapsed_ms(0, 1)
+    ex.finish_queues(600000)
+    ex.close()
+    n = cfg["n_x"] * cfg["n_y"] * cfg["n_z"]
+    return {"exact_fp32_ms_per_step": ms / steps, "exact_fp32_mlups": n * steps / (ms * 1e-3) / 1e6,
+            "exact_fp32_steps_timed": steps}
+
+
 def main():
     a = parse()
     dist = Dist()
@@ -277,7 +402,7 @@ def main():
         if dist.rank != 0:
             dist.close()
             return
-        mlups, sample, kind, cores = cpu_run(cases, max(a.steps, 1), a.ref_seconds, None)
+        mlups, sample, kind, cores = cpu_run(cpu_sample_cases(a, cases), max(a.steps, 1), a.ref_seconds, None)
         line = {"metric": metric, "value": mlups, "unit": "MLUPs/s", "n_gpus": a.gpus, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": cells / mlups / 1e3, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": workload_cfg,
@@ -301,6 +426,9 @@ def main():
         lbm.initialize()
         doms.append(lbm)
     batch = I.Batch(doms) if len(doms) > 1 else None
+    sur = None
+    if a.field_mode == "surrogate":
+        sur = surrogate_setup(a, cases[0], doms[0])
     clocks = Clocks(dist.local)
     clocks.start()
 
@@ -362,6 +490,23 @@ def main():
     tf = C.c_double()
     if mhd:
         NAT.check(NAT.lib().ion_probe_fp32_peak(C.byref(tf)))
+    if sur is not None:
+        inter = near_interactions(cfg0, doms[0].read("flags"))
+        avg = eb_ms / max(eb_n, 1)
+        tflops = inter * FLOP_PER_INTERACTION / (avg * 1e-3) / 1e12
+        roof_field = {"bound": "fp32", "achieved": tflops, "peak": tf.value, "unit": "TFLOP/s",
+                      "frac": tflops / tf.value, "traffic": None,
+                      "kernel": "learned far field phase (k_surrogate_cells near-bin sums + network + check)",
+                      "flop_per_launch": inter * FLOP_PER_INTERACTION, "interactions_per_launch": inter,
+                      "avg_launch_ms": avg, "peak_source": "measured FP32 FMA throughput (ion_probe_fp32_peak)",
+                      "note": "FLOPs counted: the exact near-bin terms only (the network adds ~2 GFLOP on tensor cores)"}
+        roofline = roof_field if eb_ms >= sc_ms else roof_stencil
+        if roofline is roof_stencil:
+            extra["roofline_field"] = roof_field
+        st = doms[0].surrogate_stats()
+        sur.update(checks_in_run=st["checks"], fallbacks_in_run=st["fallbacks"],
+                   nonfinite_checks_in_run=st["nonfinite"])
+    elif mhd:
         inter = sum(field_interactions(c["config"], d.read("flags")) for c, d in zip(cases, doms))
         if batch is None:
             avg = eb_ms / max(eb_n, 1)
@@ -376,6 +521,10 @@ def main():
                     "avg_launch_ms": avg, "peak_source": "measured FP32 FMA throughput (ion_probe_fp32_peak)"}
     if batch is not None:
         extra["autotuner"] = {"chosen": batch.chosen(), "trials": batch.tuning()}
+    if sur is not None:
+        sur.update(exact_fp32_step(cases[0], doms[0]))
+        sur["speedup_vs_exact_fp32"] = sur["exact_fp32_ms_per_step"] / (ms_max / a.steps)
+        extra["surrogate"] = sur
 
     # ---- end to end through the C ABI with host buffers ----------------------------
     e2e = None
@@ -428,8 +577,17 @@ def main():
 
     cpu = None
     if dist.rank == 0 and not a.no_cpu_baseline:
-        init = [({"b_stat": d.read("b_stat"), "flags": d.read("flags")} if mhd else {}) for d in doms]
-        mlups, sample, kind, cores = cpu_run(cases, 10 ** 6, a.ref_seconds, init)
+        ccases = cpu_sample_cases(a, cases)
+        if ccases is cases:
+            init = [({"b_stat": d.read("b_stat"), "flags": d.read("flags")} if mhd else {}) for d in doms]
+        else:  # static field of the sample box, computed on the GPU (setup, untimed)
+            init = []
+            for c in ccases:
+                d = I.Lbm(W.lbm_config(c))
+                W.apply_case(d, c)
+                init.append({"b_stat": d.read("b_stat"), "flags": d.read("flags")})
+                d.close()
+        mlups, sample, kind, cores = cpu_run(ccases, 10 ** 6, a.ref_seconds, init)
         cpu = {"value": mlups, "unit": "MLUPs/s", "cores": cores, "kind": kind, "sample": sample}
 
     if dist.rank == 0:

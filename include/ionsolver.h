@@ -242,8 +242,9 @@ int ion_lbm_reset_kernel_time(ion_lbm* h);
  *      part of update_e_b_dynamic, src/kernels/sim_kernels.cl:940-955).
  *      Per cell, LOD bins within Chebyshev distance 2 of the cell's own bin
  *      are summed exactly; the rest comes from a linear 3-D convolutional
- *      network on the LOD grid (4 channels in: q, q*v; 48 out: E and B at the
- *      8 corner cells of every block), interpolated trilinearly.  Every step a
+ *      network on the LOD grid (4 channels in: q, q*v; 168 out: E and B at
+ *      3 x 3 x 3 nodes of every block, 162 used), interpolated
+ *      triquadratically.  Every step a
  *      sampled-cell check against the exact sum decides on the device whether
  *      the exact kernel recomputes the field.  Needs ext_magneto_hydro, LOD
  *      depth >= 2 and an empty reference near field. -------------------- */
@@ -256,15 +257,24 @@ int ion_lbm_surrogate_info(ion_lbm* h, float* rel_err_fp32, float* rel_err_bf16,
                            uint32_t* epochs);
 int ion_lbm_surrogate_save(ion_lbm* h, const char* path);
 int ion_lbm_surrogate_load(ion_lbm* h, const char* path);
-/* relative tolerance of the sampled check (default 1e-2) and cells per check (default 1024) */
+/* relative tolerance of the sampled check (default 1e-2) and cells per check
+ * (default 1024); restarts the statistics and the sequence of sampled cells */
 int ion_lbm_surrogate_configure(ion_lbm* h, float tolerance, uint32_t check_cells);
-/* checks run, fallbacks taken, last relative errors of E and B */
-int ion_lbm_surrogate_stats(ion_lbm* h, uint64_t* checks, uint64_t* fallbacks, float* err_e, float* err_b);
+/* checks run, fallbacks taken, checks whose exact sample was non-finite, last
+ * relative errors of E and B.  A component that is non-finite in both the
+ * surrogate and the exact sum counts as agreeing: a non-finite source makes
+ * the exact field non-finite everywhere, so the fallback cannot repair it. */
+int ion_lbm_surrogate_stats(ion_lbm* h, uint64_t* checks, uint64_t* fallbacks, uint64_t* nonfinite, float* err_e,
+                            float* err_b);
 /* network weights (get into `out` and/or set from `in`; count = number of weights) */
 int ion_lbm_surrogate_weights(ion_lbm* h, float* out, const float* in, size_t count);
-/* loss and weight gradient of one batch: x [batch][4][V], t [batch][48][V] (host) */
+/* mean squared error and its weight gradient for one batch: x [batch][4][V],
+ * t [batch][168][V] (host, in the network's output scale) */
 int ion_lbm_surrogate_grad(ion_lbm* h, const float* x, const float* t, uint32_t batch, float* loss, float* grad);
-/* one forward pass of x [4][V] into y [48][V] (host); bf16 != 0: tensor-core path */
+/* exact far-field targets t [samples][168][V] of sources x [samples][4][V]
+ * (host), in field units; scale_e/scale_b: the network's output scales */
+int ion_lbm_surrogate_targets(ion_lbm* h, const float* x, float* t, uint32_t samples, float* scale_e, float* scale_b);
+/* one forward pass of x [4][V] into y [168][V] (host); bf16 != 0: tensor-core path */
 int ion_lbm_surrogate_forward(ion_lbm* h, const float* x, float* y, int bf16);
 /* switches the field mode of an MHD handle (ION_FIELD_*) */
 int ion_lbm_set_field_mode(ion_lbm* h, int mode);

@@ -101,8 +101,9 @@ _SIGS = {
     "ion_lbm_surrogate_save": (C.c_int, [_P, C.c_char_p]),
     "ion_lbm_surrogate_load": (C.c_int, [_P, C.c_char_p]),
     "ion_lbm_surrogate_configure": (C.c_int, [_P, C.c_float, C.c_uint32]),
-    "ion_lbm_surrogate_stats": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_float),
-                                          C.POINTER(C.c_float)]),
+    "ion_lbm_surrogate_stats": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                          C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "ion_lbm_surrogate_targets": (C.c_int, [_P, _P, _P, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "ion_lbm_surrogate_weights": (C.c_int, [_P, _P, _P, C.c_size_t]),
     "ion_lbm_surrogate_grad": (C.c_int, [_P, _P, _P, C.c_uint32, C.POINTER(C.c_float), _P]),
     "ion_lbm_surrogate_forward": (C.c_int, [_P, _P, _P, C.c_int]),

@@ -4,8 +4,7 @@
 namespace ion {
 
 void launch_lod_bins(const DevLbm& L, cudaStream_t s) {
-    const uint64_t threads = (uint64_t)L.n_lod_own * 32u;
-    k_lod_bins<<<grid_for(threads, 256), 256, 0, s>>>(L);
+    k_lod_bins<<<L.n_lod_own, LB_THREADS, 0, s>>>(L);
 }
 
 void launch_update_e_b_gated(const DevLbm& L, uint32_t* err, const uint32_t* gate, cudaStream_t s) {

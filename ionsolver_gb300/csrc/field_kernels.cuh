@@ -60,9 +60,75 @@ __device__ __forceinline__ void lod_bin_warp(const DevLbm& L, const uint32_t bin
     if (lane < 4u) L.qu_lod[(size_t)bin * 4u + lane] = acc;
 }
 
-static __global__ void __launch_bounds__(256) k_lod_bins(const DevLbm L) {
-    const uint32_t bin = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (bin < L.n_lod_own) lod_bin_warp(L, bin, threadIdx.x & 31u);
+// LOD bins of one domain, one thread block per bin: warps 1..7 stream the
+// bin's cells (ascending cell index) through shared memory in slabs of
+// LB_SLAB cells, double-buffered, while lanes 0..3 of warp 0 add charge and
+// the three velocity components one cell after another -- the same sequence
+// of float additions as lod_bin_warp.  A cell outside the fluid is stored as
+// -0.0f, which leaves every float (+0 included) unchanged under
+// round-to-nearest addition, so the sums need no branch and the summing
+// lanes read four cells per shared-memory load.
+constexpr uint32_t LB_THREADS = 256, LB_SLAB = 512;
+struct LodSmem {
+    float v[2][4][LB_SLAB];  // [buffer][component][cell]
+};
+
+static __global__ void __launch_bounds__(LB_THREADS) k_lod_bins(const DevLbm L) {
+    __shared__ __align__(16) LodSmem sm;
+    const uint32_t bin = blockIdx.x;
+    if (bin >= L.n_bins) {  // bins of the lower LOD levels stay zero (single domain)
+        if (threadIdx.x < 4u) L.qu_lod[(size_t)bin * 4u + threadIdx.x] = 0.0f;
+        return;
+    }
+    const uint32_t nd = L.nd;
+    const uint32_t bx = bin % nd, by = (bin / nd) % nd, bz = bin / (nd * nd);
+    const uint32_t cells = L.bsx * L.bsy * L.bsz;
+    const uint32_t nslabs = (cells + LB_SLAB - 1u) / LB_SLAB;
+    const size_t N = L.n;
+    auto load = [&](uint32_t k) {  // warps 1..3; the slab is padded with -0.0f to a multiple of 4 cells
+        const uint32_t base = k * LB_SLAB;
+        const uint32_t cnt = min(LB_SLAB, cells - base);
+        const uint32_t padded = (cnt + 3u) & ~3u;
+        float(*v)[LB_SLAB] = sm.v[k & 1u];
+#pragma unroll 3
+        for (uint32_t i = threadIdx.x - 32u; i < padded; i += LB_THREADS - 32u) {
+            float4 c = make_float4(-0.0f, -0.0f, -0.0f, -0.0f);
+            if (i < cnt) {  // all five loads in flight at once; the flag selects afterwards
+                const uint32_t li = base + i;
+                const uint32_t lx = li % L.bsx, ly = (li / L.bsx) % L.bsy, lz = li / (L.bsx * L.bsy);
+                const uint32_t n = (bx * L.bsx + lx) + ((by * L.bsy + ly) + (bz * L.bsz + lz) * L.ny) * L.nx;
+                const uint8_t f = L.flags[n];
+                const float4 a = make_float4(L.q[n], L.lod_cell[n], L.lod_cell[N + n], L.lod_cell[2 * N + n]);
+                if ((f & F_BO) != F_S) c = a;
+            }
+            v[0][i] = c.x; v[1][i] = c.y; v[2][i] = c.z; v[3][i] = c.w;
+        }
+    };
+    if (threadIdx.x >= 32u) load(0);
+    __syncthreads();
+    float acc = 0.0f;
+    for (uint32_t k = 0; k < nslabs; k++) {
+        if (threadIdx.x >= 32u) {
+            if (k + 1u < nslabs) load(k + 1u);
+        } else if (threadIdx.x < 4u) {
+            const uint32_t quads = (min(LB_SLAB, cells - k * LB_SLAB) + 3u) / 4u;
+            const float4* v = (const float4*)sm.v[k & 1u][threadIdx.x];
+            uint32_t i = 0;
+            for (; i + 4u <= quads; i += 4u) {  // 16 cells: loads first, then the dependent additions
+                const float4 a = v[i], b = v[i + 1u], c = v[i + 2u], d = v[i + 3u];
+                acc = acc + a.x; acc = acc + a.y; acc = acc + a.z; acc = acc + a.w;
+                acc = acc + b.x; acc = acc + b.y; acc = acc + b.z; acc = acc + b.w;
+                acc = acc + c.x; acc = acc + c.y; acc = acc + c.z; acc = acc + c.w;
+                acc = acc + d.x; acc = acc + d.y; acc = acc + d.z; acc = acc + d.w;
+            }
+            for (; i < quads; i++) {
+                const float4 a = v[i];
+                acc = acc + a.x; acc = acc + a.y; acc = acc + a.z; acc = acc + a.w;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < 4u) L.qu_lod[(size_t)bin * 4u + threadIdx.x] = acc;
 }
 
 // ---------------------------------------------------------------------------
@@ -137,12 +203,67 @@ __device__ __forceinline__ void far_fast(float cx, float cy, float cz, float4 p,
     W[0] = fmaf(inv3, w.x, W[0]); W[1] = fmaf(inv3, w.y, W[1]); W[2] = fmaf(inv3, w.z, W[2]);
 }
 
+// Packed FP32 pairs (PTX add/sub/mul/fma .f32x2, sm_100 and later): one
+// instruction does the same IEEE round-to-nearest operation on two lanes of
+// data, so two cells advance through one source with half the issue slots
+// and bit for bit the values of the scalar code.
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    float2 d;
+    asm("{.reg .b64 ra, rb, rd;\n mov.b64 ra, {%2,%3};\n mov.b64 rb, {%4,%5};\n sub.rn.f32x2 rd, ra, rb;\n"
+        " mov.b64 {%0,%1}, rd;\n}" : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+    float2 d;
+    asm("{.reg .b64 ra, rb, rd;\n mov.b64 ra, {%2,%3};\n mov.b64 rb, {%4,%5};\n mul.rn.f32x2 rd, ra, rb;\n"
+        " mov.b64 {%0,%1}, rd;\n}" : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    float2 d;
+    asm("{.reg .b64 ra, rb, rc, rd;\n mov.b64 ra, {%2,%3};\n mov.b64 rb, {%4,%5};\n mov.b64 rc, {%6,%7};\n"
+        " fma.rn.f32x2 rd, ra, rb, rc;\n mov.b64 {%0,%1}, rd;\n}"
+        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
+
+// One FAST source, pre-broadcast into pairs for far_fast2:
+// (px,px,py,py) (pz,pz,q,q) (qvx,qvx,qvy,qvy) (qvz,qvz,wx,wx) (wy,wy,wz,wz)
+struct FastSrc {
+    float4 d[5];
+};
+
+// far_fast for two cells at once (lanes .x and .y); same operations and
+// order per lane as far_fast.
+struct Pair3 {
+    float2 x, y, z;
+};
+__device__ __forceinline__ void far_fast2(const Pair3& c, const FastSrc& S, Pair3& e, Pair3& A, Pair3& W) {
+    const float4 d0 = S.d[0], d1 = S.d[1], d2 = S.d[2], d3 = S.d[3], d4 = S.d[4];
+    const float2 rx = sub2(c.x, make_float2(d0.x, d0.y));
+    const float2 ry = sub2(c.y, make_float2(d0.z, d0.w));
+    const float2 rz = sub2(c.z, make_float2(d1.x, d1.y));
+    const float2 r2 = fma2(rz, rz, fma2(ry, ry, mul2(rx, rx)));
+    float2 inv;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(inv.x) : "f"(r2.x));
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(inv.y) : "f"(r2.y));
+    const float2 inv3 = mul2(mul2(inv, inv), inv);
+    const float2 s = mul2(make_float2(d1.z, d1.w), inv3);
+    e.x = fma2(s, rx, e.x); e.y = fma2(s, ry, e.y); e.z = fma2(s, rz, e.z);
+    A.x = fma2(inv3, make_float2(d2.x, d2.y), A.x);
+    A.y = fma2(inv3, make_float2(d2.z, d2.w), A.y);
+    A.z = fma2(inv3, make_float2(d3.x, d3.y), A.z);
+    W.x = fma2(inv3, make_float2(d3.z, d3.w), W.x);
+    W.y = fma2(inv3, make_float2(d4.x, d4.y), W.y);
+    W.z = fma2(inv3, make_float2(d4.z, d4.w), W.z);
+}
+
 // Shared-memory staging area of one thread block; the mbarrier phase of each
 // buffer is tracked in `uses` so one block can process many tiles.
 struct EbSmem {
-    float4 pos[2][SRC_CHUNK];
-    float4 val[2][SRC_CHUNK];
-    float4 wv[2][SRC_CHUNK];  // FAST: qv x p of each source
+    float4 pos[2][SRC_CHUNK];  // bin centres, as copied
+    float4 val[2][SRC_CHUNK];  // (q, vx, vy, vz), as copied
+    FastSrc fast[SRC_CHUNK];   // FAST: the chunk being summed, in pairs
     uint64_t bar[2];
 };
 
@@ -156,16 +277,61 @@ __device__ __forceinline__ void eb_init(EbSmem& sm) {
 }
 
 
+// Near field of one cell: its aligned block of near_x*near_y*near_z cells
+// (sim_kernels.cl:907-938), skipping the cell itself and uncharged cells.
+template <bool FAST>
+__device__ __forceinline__ void near_field(const DevLbm& L, uint32_t n, uint32_t x, uint32_t y, uint32_t z, float* e,
+                                           float* b) {
+    const size_t N = L.n;
+    const uint32_t x0 = (x / L.near_x) * L.near_x, y0 = (y / L.near_y) * L.near_y, z0 = (z / L.near_z) * L.near_z;
+    const uint32_t x1 = min(x0 + L.near_x, L.nx), y1 = min(y0 + L.near_y, L.ny), z1 = min(z0 + L.near_z, L.nz);
+    for (uint32_t cx = x0; cx < x1; cx++)
+        for (uint32_t cy = y0; cy < y1; cy++)
+            for (uint32_t cz = z0; cz < z1; cz++) {
+                const uint32_t nc = cx + (cy + cz * L.ny) * L.nx;
+                if (nc == n) continue;
+                const float qc = L.q[nc];
+                if (qc == 0.0f) continue;
+                const float vx = L.u[nc], vy = L.u[N + nc], vz = L.u[2 * N + nc];
+                const float4 val = FAST ? make_float4(qc, qc * vx, qc * vy, qc * vz) : make_float4(qc, vx, vy, vz);
+                add_src<FAST>((float)x - (float)cx, (float)y - (float)cy, (float)z - (float)cz, val, e, b);
+            }
+}
+
+// Issues the bulk copies of source chunk c into buffer c & 1 (one thread).
+__device__ __forceinline__ void eb_issue(const DevLbm& L, EbSmem& sm, uint32_t c) {
+    const uint32_t first = L.first_src, last = L.n_lod_own;
+    const uint32_t base = first + c * SRC_CHUNK;
+    const uint32_t cnt = min(SRC_CHUNK, last - base);
+    const uint32_t buf = c & 1u;
+    mbar_expect_tx(&sm.bar[buf], 2u * cnt * 16u);
+    bulk_g2s(&sm.pos[buf][0], L.lod_pos + base, cnt * 16u, &sm.bar[buf]);
+    bulk_g2s(&sm.val[buf][0], (const float4*)L.qu_lod + base, cnt * 16u, &sm.bar[buf]);
+}
+
+__device__ __forceinline__ void eb_store(const DevLbm& L, uint32_t n, const float* e, const float* b) {
+    const size_t N = L.n;
+    L.e_dyn[n] = L.e_stat[n] + L.ke * e[0];
+    L.e_dyn[N + n] = L.e_stat[N + n] + L.ke * e[1];
+    L.e_dyn[2 * N + n] = L.e_stat[2 * N + n] + L.ke * e[2];
+    L.b_dyn[n] = L.b_stat[n] + L.kmu * b[0];
+    L.b_dyn[N + n] = L.b_stat[N + n] + L.kmu * b[1];
+    L.b_dyn[2 * N + n] = L.b_stat[2 * N + n] + L.kmu * b[2];
+}
+
 // E/B of the cells [tile, tile + EB_CPT*blockDim.x) of domain L.  Returns
 // false (block-uniform) when a staged tile did not arrive within its wait
 // limit.  Per cell the sources are added in the reference's order; the
 // cell's own bin is skipped by a check that runs only in the one source
-// chunk that can contain it.
+// chunk that can contain it.  FAST holds the cells in pairs (2j, 2j+1) and
+// advances both with packed FP32 instructions.
 template <bool FAST>
 __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t tile, EbSmem& sm, uint32_t (&uses)[2]) {
+    static_assert(EB_CPT % 2 == 0, "cells are processed in pairs");
+    constexpr uint32_t NP = EB_CPT / 2;
     const uint32_t N = L.n;
-    float fx[EB_CPT], fy[EB_CPT], fz[EB_CPT], e[EB_CPT][3], b[EB_CPT][3];
-    float Af[EB_CPT][3], Wf[EB_CPT][3];  // FAST far-field sums of the split cross product
+    float e[EB_CPT][3], b[EB_CPT][3];  // near field (and, BITWISE, everything)
+    Pair3 cp[NP], pe[NP], pA[NP], pW[NP];  // FAST far field: coordinates, E, A = sum qv/r^3, W = sum (qv x p)/r^3
     uint32_t own[EB_CPT];
     bool active[EB_CPT];
 #pragma unroll
@@ -174,95 +340,119 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t tile, Eb
         active[k] = n < N && (L.flags[n] & F_BO) != F_S;
         uint32_t x = 0, y = 0, z = 0;
         if (n < N) cell_xyz(L, n, x, y, z);
-        fx[k] = (float)x; fy[k] = (float)y; fz[k] = (float)z;
-        own[k] = n < N ? x / L.bsx + (y / L.bsy + z / L.bsz * L.nd) * L.nd : 0xFFFFFFFFu;
-        if (!active[k]) own[k] = 0xFFFFFFFFu;
+        own[k] = active[k] ? x / L.bsx + (y / L.bsy + z / L.bsz * L.nd) * L.nd : 0xFFFFFFFFu;
+        const float fx = (float)x, fy = (float)y, fz = (float)z;
+        if (k & 1u) { cp[k / 2].x.y = fx; cp[k / 2].y.y = fy; cp[k / 2].z.y = fz; }
+        else { cp[k / 2].x.x = fx; cp[k / 2].y.x = fy; cp[k / 2].z.x = fz; }
 #pragma unroll
-        for (int c = 0; c < 3; c++) { e[k][c] = 0.0f; b[k][c] = 0.0f; Af[k][c] = 0.0f; Wf[k][c] = 0.0f; }
-        // near field: the cell's aligned block (sim_kernels.cl:907-938)
-        if (active[k]) {
-            const uint32_t x0 = (x / L.near_x) * L.near_x, y0 = (y / L.near_y) * L.near_y, z0 = (z / L.near_z) * L.near_z;
-            const uint32_t x1 = min(x0 + L.near_x, L.nx), y1 = min(y0 + L.near_y, L.ny), z1 = min(z0 + L.near_z, L.nz);
-            for (uint32_t cx = x0; cx < x1; cx++)
-                for (uint32_t cy = y0; cy < y1; cy++)
-                    for (uint32_t cz = z0; cz < z1; cz++) {
-                        const uint32_t nc = cx + (cy + cz * L.ny) * L.nx;
-                        if (nc == n) continue;
-                        const float qc = L.q[nc];
-                        if (qc == 0.0f) continue;
-                        const float vx = L.u[nc], vy = L.u[(size_t)N + nc], vz = L.u[2 * (size_t)N + nc];
-                        const float4 val = FAST ? make_float4(qc, qc * vx, qc * vy, qc * vz) : make_float4(qc, vx, vy, vz);
-                        add_src<FAST>(fx[k] - (float)cx, fy[k] - (float)cy, fz[k] - (float)cz, val, e[k], b[k]);
-                    }
-        }
+        for (int c = 0; c < 3; c++) { e[k][c] = 0.0f; b[k][c] = 0.0f; }
+        if (active[k]) near_field<FAST>(L, n, x, y, z, e[k], b[k]);
+    }
+#pragma unroll
+    for (uint32_t j = 0; j < NP; j++) {
+        pe[j] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+        pA[j] = pe[j];
+        pW[j] = pe[j];
     }
 
     // depth-D LOD bins [first_src, n_lod_own) except the cell's own (sim_kernels.cl:940-955)
     const uint32_t first = L.first_src, last = L.n_lod_own;
     const uint32_t nchunks = (last - first + SRC_CHUNK - 1u) / SRC_CHUNK;
-    const float4* qu = (const float4*)L.qu_lod;
-    auto issue = [&](uint32_t c) {
-        const uint32_t base = first + c * SRC_CHUNK;
-        const uint32_t cnt = min(SRC_CHUNK, last - base);
-        const uint32_t buf = c & 1u;
-        mbar_expect_tx(&sm.bar[buf], 2u * cnt * 16u);
-        bulk_g2s(&sm.pos[buf][0], L.lod_pos + base, cnt * 16u, &sm.bar[buf]);
-        bulk_g2s(&sm.val[buf][0], qu + base, cnt * 16u, &sm.bar[buf]);
-    };
-    if (threadIdx.x == 0 && nchunks > 0) issue(0);
+    if (threadIdx.x == 0 && nchunks > 0) eb_issue(L, sm, 0);
     bool ok = true;
     uint32_t c = 0;
     for (; c < nchunks; c++) {
         const uint32_t buf = c & 1u;
-        if (threadIdx.x == 0 && c + 1 < nchunks) issue(c + 1);
+        if (threadIdx.x == 0 && c + 1 < nchunks) eb_issue(L, sm, c + 1);
         const bool landed = mbar_wait(&sm.bar[buf], uses[buf] & 1u, WAIT_LIMIT);
         ok = __syncthreads_and(landed) != 0;  // block-uniform
         if (!ok) break;
         uses[buf]++;
         const uint32_t base = first + c * SRC_CHUNK;
         const uint32_t cnt = min(SRC_CHUNK, last - base);
-        if constexpr (FAST) {  // per source: (p, q), q v and q v x p, once per tile
-            for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
-                const float4 p = sm.pos[buf][k], v = sm.val[buf][k];
-                const float qx = v.x * v.y, qy = v.x * v.z, qz = v.x * v.w;
-                sm.pos[buf][k] = make_float4(p.x, p.y, p.z, v.x);
-                sm.val[buf][k] = make_float4(qx, qy, qz, 0.0f);
-                sm.wv[buf][k] = make_float4(qy * p.z - qz * p.y, qz * p.x - qx * p.z, qx * p.y - qy * p.x, 0.0f);
-            }
-            __syncthreads();
-        }
         bool here = false;
 #pragma unroll
         for (uint32_t k = 0; k < EB_CPT; k++) here |= (own[k] - base) < cnt;
-        const float4* sp = &sm.pos[buf][0];
-        const float4* sv = &sm.val[buf][0];
-        const float4* sw = &sm.wv[buf][0];
-        if (__any_sync(0xFFFFFFFFu, here)) {  // this chunk holds some cell's own bin
-            for (uint32_t s = 0; s < cnt; s++) {
-                const float4 p = sp[s], v = sv[s];
-                if constexpr (FAST) {
-                    const float4 w = sw[s];
+        const bool any_own = __any_sync(0xFFFFFFFFu, here);  // this chunk holds some cell's own bin
+        if constexpr (FAST) {
+            // per source: q v and q v x p, broadcast into pairs (once per chunk)
+            for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
+                const float4 p = sm.pos[buf][k], v = sm.val[buf][k];
+                const float qx = v.x * v.y, qy = v.x * v.z, qz = v.x * v.w;
+                const float wx = qy * p.z - qz * p.y, wy = qz * p.x - qx * p.z, wz = qx * p.y - qy * p.x;
+                FastSrc& f = sm.fast[k];
+                f.d[0] = make_float4(p.x, p.x, p.y, p.y);
+                f.d[1] = make_float4(p.z, p.z, v.x, v.x);
+                f.d[2] = make_float4(qx, qx, qy, qy);
+                f.d[3] = make_float4(qz, qz, wx, wx);
+                f.d[4] = make_float4(wy, wy, wz, wz);
+            }
+            __syncthreads();
+            const FastSrc* fs = sm.fast;
+            if (any_own) {
+                for (uint32_t s = 0; s < cnt; s++) {
+                    const FastSrc S = fs[s];
 #pragma unroll
-                    for (uint32_t k = 0; k < EB_CPT; k++)
-                        if (base + s != own[k]) far_fast(fx[k], fy[k], fz[k], p, v, w, e[k], Af[k], Wf[k]);
-                } else {
+                    for (uint32_t j = 0; j < NP; j++) {
+                        if (base + s != own[2 * j] && base + s != own[2 * j + 1]) {
+                            far_fast2(cp[j], S, pe[j], pA[j], pW[j]);
+                        } else {  // one of the pair is in its own bin: scalar steps on the other
+                            const float4 p = make_float4(S.d[0].x, S.d[0].z, S.d[1].x, S.d[1].z);
+                            const float4 qv = make_float4(S.d[2].x, S.d[2].z, S.d[3].x, 0.0f);
+                            const float4 w = make_float4(S.d[3].z, S.d[4].x, S.d[4].z, 0.0f);
+                            const float4 pq = make_float4(p.x, p.y, p.z, S.d[1].z);
+                            if (base + s != own[2 * j]) {
+                                float ee[3] = {pe[j].x.x, pe[j].y.x, pe[j].z.x}, aa[3] = {pA[j].x.x, pA[j].y.x, pA[j].z.x},
+                                      ww[3] = {pW[j].x.x, pW[j].y.x, pW[j].z.x};
+                                far_fast(cp[j].x.x, cp[j].y.x, cp[j].z.x, pq, qv, w, ee, aa, ww);
+                                pe[j].x.x = ee[0]; pe[j].y.x = ee[1]; pe[j].z.x = ee[2];
+                                pA[j].x.x = aa[0]; pA[j].y.x = aa[1]; pA[j].z.x = aa[2];
+                                pW[j].x.x = ww[0]; pW[j].y.x = ww[1]; pW[j].z.x = ww[2];
+                            }
+                            if (base + s != own[2 * j + 1]) {
+                                float ee[3] = {pe[j].x.y, pe[j].y.y, pe[j].z.y}, aa[3] = {pA[j].x.y, pA[j].y.y, pA[j].z.y},
+                                      ww[3] = {pW[j].x.y, pW[j].y.y, pW[j].z.y};
+                                far_fast(cp[j].x.y, cp[j].y.y, cp[j].z.y, pq, qv, w, ee, aa, ww);
+                                pe[j].x.y = ee[0]; pe[j].y.y = ee[1]; pe[j].z.y = ee[2];
+                                pA[j].x.y = aa[0]; pA[j].y.y = aa[1]; pA[j].z.y = aa[2];
+                                pW[j].x.y = ww[0]; pW[j].y.y = ww[1]; pW[j].z.y = ww[2];
+                            }
+                        }
+                    }
+                }
+            } else {
+#pragma unroll 2
+                for (uint32_t s = 0; s < cnt; s++) {
+                    const FastSrc S = fs[s];
 #pragma unroll
-                    for (uint32_t k = 0; k < EB_CPT; k++)
-                        if (base + s != own[k]) add_src<false>(fx[k] - p.x, fy[k] - p.y, fz[k] - p.z, v, e[k], b[k]);
+                    for (uint32_t j = 0; j < NP; j++) far_fast2(cp[j], S, pe[j], pA[j], pW[j]);
                 }
             }
         } else {
+            const float4* sp = &sm.pos[buf][0];
+            const float4* sv = &sm.val[buf][0];
+            if (any_own) {
+                for (uint32_t s = 0; s < cnt; s++) {
+                    const float4 p = sp[s], v = sv[s];
+#pragma unroll
+                    for (uint32_t k = 0; k < EB_CPT; k++) {
+                        const Pair3& q = cp[k / 2];
+                        const float fx = (k & 1u) ? q.x.y : q.x.x, fy = (k & 1u) ? q.y.y : q.y.x,
+                                    fz = (k & 1u) ? q.z.y : q.z.x;
+                        if (base + s != own[k]) add_src<false>(fx - p.x, fy - p.y, fz - p.z, v, e[k], b[k]);
+                    }
+                }
+            } else {
 #pragma unroll 2
-            for (uint32_t s = 0; s < cnt; s++) {
-                const float4 p = sp[s], v = sv[s];
-                if constexpr (FAST) {
-                    const float4 w = sw[s];
+                for (uint32_t s = 0; s < cnt; s++) {
+                    const float4 p = sp[s], v = sv[s];
 #pragma unroll
-                    for (uint32_t k = 0; k < EB_CPT; k++) far_fast(fx[k], fy[k], fz[k], p, v, w, e[k], Af[k], Wf[k]);
-                } else {
-#pragma unroll
-                    for (uint32_t k = 0; k < EB_CPT; k++)
-                        add_src<false>(fx[k] - p.x, fy[k] - p.y, fz[k] - p.z, v, e[k], b[k]);
+                    for (uint32_t k = 0; k < EB_CPT; k++) {
+                        const Pair3& q = cp[k / 2];
+                        const float fx = (k & 1u) ? q.x.y : q.x.x, fy = (k & 1u) ? q.y.y : q.y.x,
+                                    fz = (k & 1u) ? q.z.y : q.z.x;
+                        add_src<false>(fx - p.x, fy - p.y, fz - p.z, v, e[k], b[k]);
+                    }
                 }
             }
         }
@@ -279,17 +469,20 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t tile, Eb
     for (uint32_t k = 0; k < EB_CPT; k++) {
         const uint32_t n = tile + threadIdx.x + k * blockDim.x;
         if (!active[k]) continue;
-        if constexpr (FAST) {  // B = near part + A x c - W
-            b[k][0] = b[k][0] + ((Af[k][1] * fz[k] - Af[k][2] * fy[k]) - Wf[k][0]);
-            b[k][1] = b[k][1] + ((Af[k][2] * fx[k] - Af[k][0] * fz[k]) - Wf[k][1]);
-            b[k][2] = b[k][2] + ((Af[k][0] * fy[k] - Af[k][1] * fx[k]) - Wf[k][2]);
+        if constexpr (FAST) {  // E = near part + far sum; B = near part + A x c - W
+            const uint32_t j = k / 2;
+            const bool hi = (k & 1u) != 0;
+            const float fx = hi ? cp[j].x.y : cp[j].x.x, fy = hi ? cp[j].y.y : cp[j].y.x, fz = hi ? cp[j].z.y : cp[j].z.x;
+            const float Ax = hi ? pA[j].x.y : pA[j].x.x, Ay = hi ? pA[j].y.y : pA[j].y.x, Az = hi ? pA[j].z.y : pA[j].z.x;
+            const float Wx = hi ? pW[j].x.y : pW[j].x.x, Wy = hi ? pW[j].y.y : pW[j].y.x, Wz = hi ? pW[j].z.y : pW[j].z.x;
+            e[k][0] = e[k][0] + (hi ? pe[j].x.y : pe[j].x.x);
+            e[k][1] = e[k][1] + (hi ? pe[j].y.y : pe[j].y.x);
+            e[k][2] = e[k][2] + (hi ? pe[j].z.y : pe[j].z.x);
+            b[k][0] = b[k][0] + ((Ay * fz - Az * fy) - Wx);
+            b[k][1] = b[k][1] + ((Az * fx - Ax * fz) - Wy);
+            b[k][2] = b[k][2] + ((Ax * fy - Ay * fx) - Wz);
         }
-        L.e_dyn[n] = L.e_stat[n] + L.ke * e[k][0];
-        L.e_dyn[(size_t)N + n] = L.e_stat[(size_t)N + n] + L.ke * e[k][1];
-        L.e_dyn[2 * (size_t)N + n] = L.e_stat[2 * (size_t)N + n] + L.ke * e[k][2];
-        L.b_dyn[n] = L.b_stat[n] + L.kmu * b[k][0];
-        L.b_dyn[(size_t)N + n] = L.b_stat[(size_t)N + n] + L.kmu * b[k][1];
-        L.b_dyn[2 * (size_t)N + n] = L.b_stat[2 * (size_t)N + n] + L.kmu * b[k][2];
+        eb_store(L, n, e[k], b[k]);
     }
     return true;
 }

@@ -1303,6 +1303,9 @@ static int ensure_surrogate(ion_lbm* h) {
     const uint32_t big = 1u << h->L.nd;
     if (h->L.depth < 2 || h->L.nx / big > 1 || h->L.ny / big > 1 || h->L.nz / big > 1)
         return fail(ION_E_CONFIG, "the learned far field needs LOD depth >= 2 and an empty reference near field");
+    if (h->L.bsx > (uint32_t)ion::Surrogate::MAX_BLOCK)
+        return fail(ION_E_CONFIG, "the learned far field needs LOD blocks of at most %d cells along x",
+                    ion::Surrogate::MAX_BLOCK);
     if (h->sur) return ION_OK;
     h->sur.reset(new ion::Surrogate());
     const int rc = h->sur->init((int)h->L.nd, (float)h->L.bsx, (float)h->L.bsy, (float)h->L.bsz, (int)h->L.first_src);
@@ -1356,23 +1359,26 @@ int ion_lbm_surrogate_configure(ion_lbm* h, float tolerance, uint32_t check_cell
     int rc = ensure_surrogate(h);
     if (rc) return rc;
     if (!(tolerance >= 0.0f) || check_cells == 0) return fail(ION_E_INVALID, "bad tolerance or sample count");
-    h->sur->configure(tolerance, check_cells);
+    h->sur->configure(tolerance, check_cells, h->stream);
+    CKL();
     h->graph_dirty = true;
     return ION_OK;
 }
 
-int ion_lbm_surrogate_stats(ion_lbm* h, uint64_t* checks, uint64_t* fallbacks, float* err_e, float* err_b) {
+int ion_lbm_surrogate_stats(ion_lbm* h, uint64_t* checks, uint64_t* fallbacks, uint64_t* nonfinite, float* err_e,
+                            float* err_b) {
     if (!h || !h->sur) return fail(ION_E_STATE, "no surrogate");
     unsigned long long* c;
     float* last;
     h->sur->stats_device(&c, &last);
-    unsigned long long hc[2] = {0, 0};
+    unsigned long long hc[3] = {0, 0, 0};
     float hl[2] = {0, 0};
     CK(cudaMemcpyAsync(hc, c, sizeof hc, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaMemcpyAsync(hl, last, sizeof hl, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     if (checks) *checks = hc[0];
     if (fallbacks) *fallbacks = hc[1];
+    if (nonfinite) *nonfinite = hc[2];
     if (err_e) *err_e = hl[0];
     if (err_b) *err_b = hl[1];
     return ION_OK;
@@ -1395,6 +1401,17 @@ int ion_lbm_surrogate_grad(ion_lbm* h, const float* x, const float* t, uint32_t 
     if (rc) return rc;
     rc = h->sur->grad(x, t, (int)batch, loss, grad, h->stream);
     return rc ? fail(rc, "surrogate gradient") : ION_OK;
+}
+
+int ion_lbm_surrogate_targets(ion_lbm* h, const float* x, float* t, uint32_t samples, float* scale_e, float* scale_b) {
+    if (!h || !x || !t || samples == 0) return fail(ION_E_INVALID, "null argument");
+    int rc = ensure_surrogate(h);
+    if (rc) return rc;
+    rc = h->sur->targets(x, t, (int)samples, h->stream);
+    if (rc) return fail(rc, "surrogate targets");
+    if (scale_e) *scale_e = h->sur->out_scale_e();
+    if (scale_b) *scale_b = h->sur->out_scale_b();
+    return ION_OK;
 }
 
 int ion_lbm_surrogate_forward(ion_lbm* h, const float* x, float* y, int bf16) {

@@ -3,22 +3,23 @@
 // IonSolver src/kernels/sim_kernels.cl:940-955).
 //
 // Split of the reference's sum over the depth-D LOD bins of one cell:
-//   near : bins within Chebyshev distance R_NEAR (= 2) of the cell's own bin
+//   near : bins within Chebyshev distance RNEAR (= 2) of the cell's own bin
 //          (own bin excluded, as the reference excludes it) -- summed exactly
-//          per cell (<= 124 terms instead of ~3511);
+//          per cell (<= 124 terms instead of ~4095);
 //   far  : all other bins in range -- smooth over one block, so it is taken
-//          at the 8 corner cells of the cell's block and interpolated
-//          trilinearly.  The 8 x 6 corner values of every block come from a
+//          at 3 x 3 x 3 nodes of the cell's block (corners, edge and face
+//          midpoints, centre) and interpolated with triquadratic Lagrange
+//          weights.  The 27 x 6 node values of every block come from a
 //          bias-free (linear) 3-D convolutional network on the LOD grid:
 //          4 input channels (q, q vx, q vy, q vz per bin), 32 hidden
 //          channels, 4 residual blocks of two 3^3 convolutions (dilations
-//          (1,2) (2,4) (4,8) (1,1)), 48 output channels.  The target map is
-//          linear in the sources, so the network is kept linear: scaling the
-//          inputs scales the outputs exactly.
+//          (1,2) (2,4) (4,8) (1,1)), 168 output channels (162 used).  The
+//          target map is linear in the sources, so the network is kept
+//          linear: scaling the inputs scales the outputs exactly.
 // Training runs on the GPU with the kernels below (FP32 forward, backward
 // of data and weights, Adam); inference runs in BF16 on the tensor cores
 // (mma.sync m16n8k16, FP32 accumulation).  Each step a sampled-cell check
-// compares the surrogate against the exact sum on a few cells; above the
+// compares the written field with the exact sum on a few cells; above the
 // tolerance the exact kernel recomputes the whole field.
 #include <cmath>
 #include <cstdio>
@@ -40,42 +41,55 @@ namespace ion {
 __device__ __forceinline__ int tap_off(int k, int a) { return (a == 0 ? k % 3 : a == 1 ? (k / 3) % 3 : k / 9) - 1; }
 
 // ---------------------------------------------------------------------------
-// exact far-field targets at the 8 corner cells of every block
+// exact far-field targets at the 27 nodes of every block
 //   src [4][V]: (q, qvx, qvy, qvz) per bin (bins below first_src are 0)
-//   out [48][V]: channel = corner * 6 + component (Ex,Ey,Ez,Bx,By,Bz)
+//   out [OUT_PAD][V]: channel = node * 6 + component (Ex,Ey,Ez,Bx,By,Bz),
+//   node = ix + 3 (iy + 3 iz) at cell offset (i / 2) (bs - 1) on each axis;
+//   channels >= OUT_CH are left as they are (zero).
+// FP32 with IEEE sqrt and divide; the sum runs over bins in ascending order.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_far_targets(const float* src, int nd, float bs_x, float bs_y, float bs_z,
                                                      int rnear, float* out, int nsamples) {
+    constexpr int NODES = Surrogate::NODES;
     const int V = nd * nd * nd;
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (long long)V * 8 * nsamples) return;
-    const int s = (int)(gid / (V * 8));
-    const int r = (int)(gid % (V * 8));
-    const int v = r / 8, corner = r % 8;
+    if (gid >= (long long)V * NODES * nsamples) return;
+    const int s = (int)(gid / (V * NODES));
+    const int r = (int)(gid % (V * NODES));
+    const int v = r / NODES, node = r % NODES;
     const int bx = v % nd, by = (v / nd) % nd, bz = v / (nd * nd);
-    // corner cell coordinates (cells are at integer positions, bin centres at (i + 1/2) bs)
-    const float px = bx * bs_x + ((corner & 1) ? bs_x - 1.0f : 0.0f);
-    const float py = by * bs_y + ((corner & 2) ? bs_y - 1.0f : 0.0f);
-    const float pz = bz * bs_z + ((corner & 4) ? bs_z - 1.0f : 0.0f);
+    const float tx = 0.5f * (float)(node % 3), ty = 0.5f * (float)((node / 3) % 3), tz = 0.5f * (float)(node / 9);
+    const float px = bx * bs_x + tx * (bs_x - 1.0f);
+    const float py = by * bs_y + ty * (bs_y - 1.0f);
+    const float pz = bz * bs_z + tz * (bs_z - 1.0f);
     const float* S = src + (size_t)s * 4 * V;
-    double e[3] = {0, 0, 0}, b[3] = {0, 0, 0};
+    float e[3] = {0, 0, 0}, b[3] = {0, 0, 0};
     for (int d = 0; d < V; d++) {
         const int dx = d % nd, dy = (d / nd) % nd, dz = d / (nd * nd);
         const int cheb = max(abs(dx - bx), max(abs(dy - by), abs(dz - bz)));
         if (cheb <= rnear) continue;
         const float q = S[d];
         const float qx = S[V + d], qy = S[2 * V + d], qz = S[3 * V + d];
-        const double Rx = px - (dx + 0.5) * bs_x, Ry = py - (dy + 0.5) * bs_y, Rz = pz - (dz + 0.5) * bs_z;
-        const double r2 = Rx * Rx + Ry * Ry + Rz * Rz;
-        const double inv3 = 1.0 / (r2 * sqrt(r2));
+        const float Rx = px - (dx * bs_x + 0.5f * bs_x), Ry = py - (dy * bs_y + 0.5f * bs_y);
+        const float Rz = pz - (dz * bs_z + 0.5f * bs_z);
+        const float r2 = Rx * Rx + Ry * Ry + Rz * Rz;
+        const float inv3 = 1.0f / (r2 * sqrtf(r2));
         e[0] += q * Rx * inv3; e[1] += q * Ry * inv3; e[2] += q * Rz * inv3;
         b[0] += (qy * Rz - qz * Ry) * inv3; b[1] += (qz * Rx - qx * Rz) * inv3; b[2] += (qx * Ry - qy * Rx) * inv3;
     }
-    float* O = out + (size_t)s * 48 * V;
+    float* O = out + (size_t)s * Surrogate::OUT_PAD * V;
     for (int c = 0; c < 3; c++) {
-        O[(corner * 6 + c) * V + v] = (float)e[c];
-        O[(corner * 6 + 3 + c) * V + v] = (float)b[c];
+        O[(node * 6 + c) * V + v] = e[c];
+        O[(node * 6 + 3 + c) * V + v] = b[c];
     }
+}
+
+// divides the E channels by yE and the B channels by yB (network output scale)
+__global__ void k_scale_targets(float* T, int V, size_t total, float inv_e, float inv_b) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const int ch = (int)((i / V) % Surrogate::OUT_PAD);
+    T[i] *= (ch % 6 < 3) ? inv_e : inv_b;
 }
 
 // ---------------------------------------------------------------------------
@@ -84,32 +98,43 @@ __global__ void __launch_bounds__(256) k_far_targets(const float* src, int nd, f
 constexpr int COG = 8;  // output channels per thread
 
 // out[b][co][v] = (res ? res[b][co][v] : 0) + sum_ci sum_k w[co][ci][k] in[b][ci][v + dil*off_k]
+// (weights staged through shared memory CI_CHUNK input channels at a time)
+constexpr int CI_CHUNK = 32;
 __global__ void __launch_bounds__(128) k_conv_fwd(const float* in, const float* w, const float* res, float* out, int Cin,
                                                   int Cout, int dil, int nd, int B) {
-    extern __shared__ float sw[];  // [COG][Cin][27]
+    __shared__ float sw[COG * CI_CHUNK * 27];
     const int V = nd * nd * nd;
     const int co0 = blockIdx.y * COG;
     const int ncog = min(COG, Cout - co0);
-    for (int i = threadIdx.x; i < ncog * Cin * 27; i += blockDim.x) sw[i] = w[(size_t)co0 * Cin * 27 + i];
-    __syncthreads();
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (long long)B * V) return;
-    const int b = (int)(gid / V), v = (int)(gid % V);
+    const bool live = gid < (long long)B * V;
+    const int b = live ? (int)(gid / V) : 0, v = live ? (int)(gid % V) : 0;
     const int x = v % nd, y = (v / nd) % nd, z = v / (nd * nd);
     float acc[COG];
 #pragma unroll
     for (int j = 0; j < COG; j++) acc[j] = 0.0f;
     const float* I = in + (size_t)b * Cin * V;
-    for (int k = 0; k < 27; k++) {
-        const int xx = x + dil * tap_off(k, 0), yy = y + dil * tap_off(k, 1), zz = z + dil * tap_off(k, 2);
-        if (xx < 0 || yy < 0 || zz < 0 || xx >= nd || yy >= nd || zz >= nd) continue;
-        const int nv = xx + (yy + zz * nd) * nd;
-        for (int ci = 0; ci < Cin; ci++) {
-            const float a = I[(size_t)ci * V + nv];
+    for (int ci0 = 0; ci0 < Cin; ci0 += CI_CHUNK) {
+        const int nci = min(CI_CHUNK, Cin - ci0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < ncog * nci * 27; i += blockDim.x) {
+            const int j = i / (nci * 27), r = i % (nci * 27);
+            sw[(j * CI_CHUNK + r / 27) * 27 + r % 27] = w[((size_t)(co0 + j) * Cin + ci0 + r / 27) * 27 + r % 27];
+        }
+        __syncthreads();
+        if (!live) continue;
+        for (int k = 0; k < 27; k++) {
+            const int xx = x + dil * tap_off(k, 0), yy = y + dil * tap_off(k, 1), zz = z + dil * tap_off(k, 2);
+            if (xx < 0 || yy < 0 || zz < 0 || xx >= nd || yy >= nd || zz >= nd) continue;
+            const int nv = xx + (yy + zz * nd) * nd;
+            for (int ci = 0; ci < nci; ci++) {
+                const float a = I[(size_t)(ci0 + ci) * V + nv];
 #pragma unroll
-            for (int j = 0; j < COG; j++) acc[j] = fmaf(sw[(j * Cin + ci) * 27 + k], a, acc[j]);
+                for (int j = 0; j < COG; j++) acc[j] = fmaf(sw[(j * CI_CHUNK + ci) * 27 + k], a, acc[j]);
+            }
         }
     }
+    if (!live) return;
     for (int j = 0; j < ncog; j++) {
         const size_t o = ((size_t)b * Cout + co0 + j) * V + v;
         out[o] = (res ? res[o] : 0.0f) + acc[j];
@@ -195,99 +220,92 @@ __global__ void k_adam(float* w, const float* g, float* m, float* v, size_t n, f
 
 // ---------------------------------------------------------------------------
 // BF16 tensor-core inference: implicit GEMM per layer, M = voxels, N = Cout,
-// K = Cin*27, mma.sync.m16n8k16 (BF16 in, FP32 accumulate).
-//   act [Cin][V] bf16 (one sample), wk [K][Cout] bf16 with k = tap*Cin + ci
-//   out fp32 [Cout][V] (+ res), outb bf16 copy for the next layer
-// One warp computes 16 voxels x all Cout (Cout / 8 n-tiles).
+// K = 27 taps x CIN channels (k = tap * CIN + ci), mma.sync.m16n8k16 (BF16 in,
+// FP32 accumulate).  Activations are voxel-major, act [V][CIN] bf16, so the
+// two K-neighbours of an A fragment register are one 32-bit load; weights are
+// packed wkT [Cout][K] bf16 for the same reason on B.  The 4 input channels
+// of the first layer are padded to 16.
+//   out fp32 [Cout][V] (+ res), outb bf16 [V][Cout] copy for the next layer
+// One warp computes 16 voxels x NTW n-tiles of 8 channels; blockIdx.y picks
+// the group of n-tiles.
 // ---------------------------------------------------------------------------
-template <int NT>  // n-tiles of 8 output channels
-__global__ void __launch_bounds__(128) k_conv_bf16(const __nv_bfloat16* act, const __nv_bfloat16* wk, const float* res,
-                                                   float* out, __nv_bfloat16* outb, int Cin, int dil, int nd) {
+__device__ __forceinline__ uint32_t ld_b32(const __nv_bfloat16* p) { return *(const uint32_t*)p; }
+
+template <int CIN, int NTW>
+__global__ void __launch_bounds__(128) k_conv_bf16(const __nv_bfloat16* act, const __nv_bfloat16* wkT, const float* res,
+                                                   float* out, __nv_bfloat16* outb, int Cout, int dil, int nd) {
+    static_assert(CIN % 16 == 0, "K steps of 16 stay within one tap");
+    constexpr int K = 27 * CIN;
     const int V = nd * nd * nd;
-    const int Cout = NT * 8;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     const int g = lane >> 2, tg = lane & 3;
     const int v0 = warp * 16;
     if (v0 >= V) return;
-    float acc[NT][4];
+    const int nt0 = blockIdx.y * NTW;
+    float acc[NTW][4];
 #pragma unroll
-    for (int t = 0; t < NT; t++) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.0f;
+    for (int t = 0; t < NTW; t++) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.0f;
     // voxel rows owned by this thread in the A fragment: v0 + g and v0 + g + 8
     const int va = v0 + g, vb = v0 + g + 8;
     const int xa = va % nd, ya = (va / nd) % nd, za = va / (nd * nd);
     const int xb = vb % nd, yb = (vb / nd) % nd, zb = vb / (nd * nd);
-    const int K = Cin * 27;
-    for (int k0 = 0; k0 < K; k0 += 16) {
-        // A fragment: rows (va, vb), cols k0 + tg*2 + {0,1} and k0 + 8 + tg*2 + {0,1}
-        uint32_t a[4];
+    const __nv_bfloat16* wrow[NTW];
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
+    for (int t = 0; t < NTW; t++) wrow[t] = wkT + (size_t)((nt0 + t) * 8 + g) * K + tg * 2;
+    for (int tap = 0; tap < 27; tap++) {
+        const int ox = dil * tap_off(tap, 0), oy = dil * tap_off(tap, 1), oz = dil * tap_off(tap, 2);
+        const int ax = xa + ox, ay = ya + oy, az = za + oz, bx = xb + ox, by = yb + oy, bz = zb + oz;
+        const bool ina = ax >= 0 && ay >= 0 && az >= 0 && ax < nd && ay < nd && az < nd;
+        const bool inb = bx >= 0 && by >= 0 && bz >= 0 && bx < nd && by < nd && bz < nd;
+        const __nv_bfloat16* pa = act + (size_t)(ina ? ax + (ay + az * nd) * nd : 0) * CIN + tg * 2;
+        const __nv_bfloat16* pb = act + (size_t)(inb ? bx + (by + bz * nd) * nd : 0) * CIN + tg * 2;
 #pragma unroll
-            for (int rsel = 0; rsel < 2; rsel++) {
-                __nv_bfloat16 pair[2];
+        for (int c0 = 0; c0 < CIN; c0 += 16) {
+            // a0:(g, k lo) a1:(g+8, k lo) a2:(g, k hi) a3:(g+8, k hi)
+            const uint32_t a0 = ina ? ld_b32(pa + c0) : 0u, a1 = inb ? ld_b32(pb + c0) : 0u;
+            const uint32_t a2 = ina ? ld_b32(pa + c0 + 8) : 0u, a3 = inb ? ld_b32(pb + c0 + 8) : 0u;
+            const int k0 = tap * CIN + c0;
 #pragma unroll
-                for (int e = 0; e < 2; e++) {
-                    const int kk = k0 + h * 8 + tg * 2 + e;
-                    const int tap = kk / Cin, ci = kk % Cin;
-                    const int x = (rsel ? xb : xa) + dil * tap_off(tap, 0);
-                    const int y = (rsel ? yb : ya) + dil * tap_off(tap, 1);
-                    const int z = (rsel ? zb : za) + dil * tap_off(tap, 2);
-                    const bool in = kk < K && x >= 0 && y >= 0 && z >= 0 && x < nd && y < nd && z < nd;
-                    pair[e] = in ? act[(size_t)ci * V + x + (y + z * nd) * nd] : __float2bfloat16(0.0f);
-                }
-                uint32_t u;
-                memcpy(&u, pair, 4);
-                a[h * 2 + rsel] = u;  // a0:(g,k lo) a1:(g+8,k lo) a2:(g,k hi) a3:(g+8,k hi)
+            for (int t = 0; t < NTW; t++) {
+                const uint32_t b0 = ld_b32(wrow[t] + k0), b1 = ld_b32(wrow[t] + k0 + 8);
+                asm volatile(
+                    "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                    "{%0,%1,%2,%3};\n"
+                    : "+f"(acc[t][0]), "+f"(acc[t][1]), "+f"(acc[t][2]), "+f"(acc[t][3])
+                    : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
             }
-        }
-#pragma unroll
-        for (int t = 0; t < NT; t++) {
-            // B fragment: k rows tg*2+{0,1} (+8), column n = t*8 + g
-            __nv_bfloat16 b0[2], b1[2];
-#pragma unroll
-            for (int e = 0; e < 2; e++) {
-                const int ka = k0 + tg * 2 + e, kb = k0 + 8 + tg * 2 + e;
-                b0[e] = ka < K ? wk[(size_t)ka * Cout + t * 8 + g] : __float2bfloat16(0.0f);
-                b1[e] = kb < K ? wk[(size_t)kb * Cout + t * 8 + g] : __float2bfloat16(0.0f);
-            }
-            uint32_t ub0, ub1;
-            memcpy(&ub0, b0, 4);
-            memcpy(&ub1, b1, 4);
-            asm volatile(
-                "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-                "{%0,%1,%2,%3};\n"
-                : "+f"(acc[t][0]), "+f"(acc[t][1]), "+f"(acc[t][2]), "+f"(acc[t][3])
-                : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(ub0), "r"(ub1));
         }
     }
     // C fragment: (g, n = t*8 + tg*2 + {0,1}) and (g+8, same n)
 #pragma unroll
-    for (int t = 0; t < NT; t++) {
+    for (int t = 0; t < NTW; t++) {
 #pragma unroll
         for (int e = 0; e < 4; e++) {
             const int v = (e < 2) ? va : vb;
-            const int n = t * 8 + tg * 2 + (e & 1);
+            const int n = (nt0 + t) * 8 + tg * 2 + (e & 1);
             const size_t o = (size_t)n * V + v;
             const float val = acc[t][e] + (res ? res[o] : 0.0f);
             out[o] = val;
-            if (outb) outb[o] = __float2bfloat16(val);
+            if (outb) outb[(size_t)v * Cout + n] = __float2bfloat16(val);
         }
     }
-    (void)Cout;
 }
 
-__global__ void k_to_bf16(const float* x, __nv_bfloat16* y, size_t n) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) y[i] = __float2bfloat16(x[i]);
-}
-
-// wk[(tap*Cin + ci)][co] = w[co][ci][tap]
-__global__ void k_pack_weights(const float* w, __nv_bfloat16* wk, int Cin, int Cout) {
+// network input in the inference layout: act [V][16] bf16, channels 4..15 zero
+__global__ void k_input_bf16(const float* X, __nv_bfloat16* act, int V) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= Cin * Cout * 27) return;
-    const int co = i % Cout, kk = i / Cout, tap = kk / Cin, ci = kk % Cin;
-    wk[i] = __float2bfloat16(w[((size_t)co * Cin + ci) * 27 + tap]);
+    if (i >= V * 16) return;
+    const int v = i / 16, c = i % 16;
+    act[i] = __float2bfloat16(c < 4 ? X[(size_t)c * V + v] : 0.0f);
+}
+
+// wkT[co][tap * cinp + ci] = w[co][ci][tap] (zero for the padding channels ci >= cin)
+__global__ void k_pack_weights(const float* w, __nv_bfloat16* wkT, int cin, int cinp, int cout) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cout * 27 * cinp) return;
+    const int co = i / (27 * cinp), k = i % (27 * cinp), tap = k / cinp, ci = k % cinp;
+    wkT[i] = __float2bfloat16(ci < cin ? w[((size_t)co * cin + ci) * 27 + tap] : 0.0f);
 }
 
 // scales of the current sources: max |q| and max |q v| over the bins in range
@@ -316,96 +334,227 @@ __global__ void k_source_scale(const float* qu_lod, int V, int first, float* sca
 }
 
 // ---------------------------------------------------------------------------
-// per-cell field from the surrogate: exact near bins + interpolated far field
-// Y [48][V] network output (normalised); scale: (sq*yE, sv*yB) from device
+// per-cell field from the surrogate: exact near bins + interpolated far field.
+// One thread block per bin, walking the bin's cells in tiles of SC_CELLS:
+// all of them share the bin's list of near sources (shared memory, ascending
+// bin order, built once) and its 27 x 6 node values.  Near sums use the FAST
+// arithmetic in packed pairs (far_fast2).
+//   Y [OUT_PAD][V] network output (normalised); scales: (sq, sv) from the device
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_surrogate_cells(const DevLbm L, const float* Y, const float* scales, float yE,
-                                                         float yB, int rnear) {
-    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= L.n || (L.flags[n] & F_BO) == F_S) return;
-    uint32_t x, y, z;
-    cell_xyz(L, n, x, y, z);
+constexpr uint32_t SC_CPT = 4, SC_THREADS = 256, SC_CELLS = SC_CPT * SC_THREADS;
+struct SurSmem {
+    FastSrc src[125];
+    float node[Surrogate::OUT_CH];
+    // node values contracted along x: t1[lx][iy + 3 iz][c] = sum_ix wx_ix(lx) node[ix + 3 (iy + 3 iz)][c]
+    float4 t1[Surrogate::MAX_BLOCK][9][2];
+    uint32_t count;
+};
+
+__device__ __forceinline__ void quad_weights(float t, float* w) {  // Lagrange weights of the nodes 0, 1/2, 1
+    w[0] = 2.0f * (t - 0.5f) * (t - 1.0f);
+    w[1] = -4.0f * t * (t - 1.0f);
+    w[2] = 2.0f * t * (t - 0.5f);
+}
+
+__device__ __forceinline__ void surrogate_tile(const DevLbm& L, const SurSmem& sm, uint32_t bin, int bx, int by, int bz,
+                                               uint32_t tile, uint32_t cells, float sE, float sB);
+
+__global__ void __launch_bounds__(SC_THREADS) k_surrogate_cells(const DevLbm L, const float* Y, const float* scales,
+                                                                float yE, float yB) {
+    __shared__ __align__(16) SurSmem sm;
+    const uint32_t bin = blockIdx.x;
     const int nd = (int)L.nd, V = nd * nd * nd;
-    const int bx = (int)(x / L.bsx), by = (int)(y / L.bsy), bz = (int)(z / L.bsz);
-    const int own = bx + (by + bz * nd) * nd;
-    const float fx = (float)x, fy = (float)y, fz = (float)z;
-    float e[3] = {0, 0, 0}, b[3] = {0, 0, 0};
-    const float4* qu = (const float4*)L.qu_lod;
-    for (int dz = max(bz - rnear, 0); dz <= min(bz + rnear, nd - 1); dz++)
-        for (int dy = max(by - rnear, 0); dy <= min(by + rnear, nd - 1); dy++)
-            for (int dx = max(bx - rnear, 0); dx <= min(bx + rnear, nd - 1); dx++) {
-                const int d = dx + (dy + dz * nd) * nd;
-                if (d == own || (uint32_t)d < L.first_src) continue;
+    const int bx = (int)bin % nd, by = ((int)bin / nd) % nd, bz = (int)bin / (nd * nd);
+    if (threadIdx.x < 32) {  // near sources in ascending bin index (offsets in z, y, x order)
+        const uint32_t lane = threadIdx.x;
+        const float4* qu = (const float4*)L.qu_lod;
+        uint32_t cnt = 0;
+        for (int o0 = 0; o0 < 125; o0 += 32) {
+            const int o = o0 + (int)lane;
+            const int x = bx + o % 5 - 2, y = by + (o / 5) % 5 - 2, z = bz + o / 25 - 2;
+            const int d = x + (y + z * nd) * nd;
+            const bool ok = o < 125 && x >= 0 && y >= 0 && z >= 0 && x < nd && y < nd && z < nd && d != (int)bin &&
+                            (uint32_t)d >= L.first_src;
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, ok);
+            if (ok) {
                 const float4 p = L.lod_pos[d], v = qu[d];
-                add_src<true>(fx - p.x, fy - p.y, fz - p.z, make_float4(v.x, v.x * v.y, v.x * v.z, v.x * v.w), e, b);
+                const float qx = v.x * v.y, qy = v.x * v.z, qz = v.x * v.w;
+                const float wx = qy * p.z - qz * p.y, wy = qz * p.x - qx * p.z, wz = qx * p.y - qy * p.x;
+                FastSrc& f = sm.src[cnt + __popc(m & ((1u << lane) - 1u))];
+                f.d[0] = make_float4(p.x, p.x, p.y, p.y);
+                f.d[1] = make_float4(p.z, p.z, v.x, v.x);
+                f.d[2] = make_float4(qx, qx, qy, qy);
+                f.d[3] = make_float4(qz, qz, wx, wx);
+                f.d[4] = make_float4(wy, wy, wz, wz);
             }
-    // trilinear weights within the block (corner cells at offsets 0 and bs-1)
-    const float tx = L.bsx > 1 ? (float)(x - bx * L.bsx) / (float)(L.bsx - 1) : 0.0f;
-    const float ty = L.bsy > 1 ? (float)(y - by * L.bsy) / (float)(L.bsy - 1) : 0.0f;
-    const float tz = L.bsz > 1 ? (float)(z - bz * L.bsz) / (float)(L.bsz - 1) : 0.0f;
-    float far[6] = {0, 0, 0, 0, 0, 0};
-#pragma unroll
-    for (int c = 0; c < 8; c++) {
-        const float wgt = ((c & 1) ? tx : 1.0f - tx) * ((c & 2) ? ty : 1.0f - ty) * ((c & 4) ? tz : 1.0f - tz);
-#pragma unroll
-        for (int k = 0; k < 6; k++) far[k] = fmaf(wgt, Y[(size_t)(c * 6 + k) * V + own], far[k]);
+            cnt += __popc(m);
+        }
+        if (lane == 0) sm.count = cnt;
     }
+    for (uint32_t i = threadIdx.x; i < (uint32_t)Surrogate::OUT_CH; i += blockDim.x) sm.node[i] = Y[(size_t)i * V + bin];
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < L.bsx * 9u * 8u; i += blockDim.x) {
+        const uint32_t lx = i / 72u, jk = (i / 8u) % 9u, c = i % 8u;
+        float wx[3];
+        quad_weights(L.bsx > 1 ? (float)lx / (float)(L.bsx - 1) : 0.0f, wx);
+        float v = 0.0f;
+        if (c < 6u)
+            for (int ix = 0; ix < 3; ix++) v = fmaf(wx[ix], sm.node[(ix + 3 * jk) * 6 + c], v);
+        ((float*)&sm.t1[lx][jk][0])[c] = v;
+    }
+    __syncthreads();
+
+    const uint32_t cells = L.bsx * L.bsy * L.bsz;
     const float sE = scales[0] * yE, sB = scales[1] * yB;
+    for (uint32_t tile = 0; tile * SC_CELLS < cells; tile++)
+        surrogate_tile(L, sm, bin, bx, by, bz, tile, cells, sE, sB);
+}
+
+__device__ __forceinline__ void surrogate_tile(const DevLbm& L, const SurSmem& sm, uint32_t bin, int bx, int by, int bz,
+                                               uint32_t tile, uint32_t cells, float sE, float sB) {
+    // cell k of this thread: local index li -> (lx, ly, lz) in the bin -> global (x, y, z)
+    auto cell = [&](uint32_t k, uint32_t& lx, uint32_t& ly, uint32_t& lz) -> uint32_t {
+        const uint32_t li = tile * SC_CELLS + threadIdx.x + k * SC_THREADS;
+        const uint32_t lc = li < cells ? li : 0u;
+        lx = lc % L.bsx; ly = (lc / L.bsx) % L.bsy; lz = lc / (L.bsx * L.bsy);
+        return li;
+    };
+    Pair3 cp[SC_CPT / 2], pe[SC_CPT / 2], pA[SC_CPT / 2], pW[SC_CPT / 2];
+    uint32_t live = 0u;  // bit k: cell k exists and is not solid
     const size_t N = L.n;
-    L.e_dyn[n] = L.e_stat[n] + L.ke * (e[0] + sE * far[0]);
-    L.e_dyn[N + n] = L.e_stat[N + n] + L.ke * (e[1] + sE * far[1]);
-    L.e_dyn[2 * N + n] = L.e_stat[2 * N + n] + L.ke * (e[2] + sE * far[2]);
-    L.b_dyn[n] = L.b_stat[n] + L.kmu * (b[0] + sB * far[3]);
-    L.b_dyn[N + n] = L.b_stat[N + n] + L.kmu * (b[1] + sB * far[4]);
-    L.b_dyn[2 * N + n] = L.b_stat[2 * N + n] + L.kmu * (b[2] + sB * far[5]);
+#pragma unroll
+    for (uint32_t k = 0; k < SC_CPT; k++) {
+        uint32_t lx, ly, lz;
+        const uint32_t li = cell(k, lx, ly, lz);
+        const uint32_t x = bx * L.bsx + lx, y = by * L.bsy + ly, z = bz * L.bsz + lz;
+        const uint32_t m = x + (y + z * L.ny) * L.nx;
+        if (li < cells && (L.flags[m] & F_BO) != F_S) live |= 1u << k;
+        // the static fields are read after the near sums: start them towards L2 now
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(L.e_stat + c * N + m));
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(L.b_stat + c * N + m));
+        }
+        float2& cx = cp[k / 2].x; float2& cy = cp[k / 2].y; float2& cz = cp[k / 2].z;
+        if (k & 1u) { cx.y = (float)x; cy.y = (float)y; cz.y = (float)z; }
+        else { cx.x = (float)x; cy.x = (float)y; cz.x = (float)z; }
+    }
+#pragma unroll
+    for (uint32_t j = 0; j < SC_CPT / 2; j++) {
+        pe[j] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+        pA[j] = pe[j];
+        pW[j] = pe[j];
+    }
+    const uint32_t cnt = sm.count;
+#pragma unroll 1
+    for (uint32_t s = 0; s < cnt; s++) {
+        const FastSrc S = sm.src[s];
+#pragma unroll
+        for (uint32_t j = 0; j < SC_CPT / 2; j++) far_fast2(cp[j], S, pe[j], pA[j], pW[j]);
+    }
+#pragma unroll
+    for (uint32_t k = 0; k < SC_CPT; k++) {
+        if (!(live & (1u << k))) continue;
+        uint32_t lx, ly, lz;
+        cell(k, lx, ly, lz);
+        const uint32_t m = (bx * L.bsx + lx) + ((by * L.bsy + ly) + (bz * L.bsz + lz) * L.ny) * L.nx;
+        const uint32_t j = k / 2;
+        const bool hi = (k & 1u) != 0;
+        const float fx = hi ? cp[j].x.y : cp[j].x.x, fy = hi ? cp[j].y.y : cp[j].y.x, fz = hi ? cp[j].z.y : cp[j].z.x;
+        const float Ax = hi ? pA[j].x.y : pA[j].x.x, Ay = hi ? pA[j].y.y : pA[j].y.x, Az = hi ? pA[j].z.y : pA[j].z.x;
+        const float Wx = hi ? pW[j].x.y : pW[j].x.x, Wy = hi ? pW[j].y.y : pW[j].y.x, Wz = hi ? pW[j].z.y : pW[j].z.x;
+        const float e[3] = {hi ? pe[j].x.y : pe[j].x.x, hi ? pe[j].y.y : pe[j].y.x, hi ? pe[j].z.y : pe[j].z.x};
+        const float b[3] = {(Ay * fz - Az * fy) - Wx, (Az * fx - Ax * fz) - Wy, (Ax * fy - Ay * fx) - Wz};
+        // triquadratic interpolation: the x contraction is tabulated per bin (t1)
+        float wy[3], wz[3];
+        quad_weights(L.bsy > 1 ? (float)ly / (float)(L.bsy - 1) : 0.0f, wy);
+        quad_weights(L.bsz > 1 ? (float)lz / (float)(L.bsz - 1) : 0.0f, wz);
+        float far[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+        for (int jk = 0; jk < 9; jk++) {
+            const float wgt = wy[jk % 3] * wz[jk / 3];
+            const float4 a = sm.t1[lx][jk][0], b2 = sm.t1[lx][jk][1];
+            far[0] = fmaf(wgt, a.x, far[0]); far[1] = fmaf(wgt, a.y, far[1]); far[2] = fmaf(wgt, a.z, far[2]);
+            far[3] = fmaf(wgt, a.w, far[3]); far[4] = fmaf(wgt, b2.x, far[4]); far[5] = fmaf(wgt, b2.y, far[5]);
+        }
+        L.e_dyn[m] = L.e_stat[m] + L.ke * (e[0] + sE * far[0]);
+        L.e_dyn[N + m] = L.e_stat[N + m] + L.ke * (e[1] + sE * far[1]);
+        L.e_dyn[2 * N + m] = L.e_stat[2 * N + m] + L.ke * (e[2] + sE * far[2]);
+        L.b_dyn[m] = L.b_stat[m] + L.kmu * (b[0] + sB * far[3]);
+        L.b_dyn[N + m] = L.b_stat[N + m] + L.kmu * (b[1] + sB * far[4]);
+        L.b_dyn[2 * N + m] = L.b_stat[2 * N + m] + L.kmu * (b[2] + sB * far[5]);
+    }
 }
 
 // ---------------------------------------------------------------------------
-// sampled exact check: exact dynamic E/B (FAST arithmetic, full bin range)
-// on `count` cells picked by a hash of the step, compared with the values the
-// surrogate wrote.  stats[0] = max |dE|, [1] = max |E|, [2] = max |dB|, [3] = max |B|
-// (as float bits, atomicMax on non-negative floats)
+// sampled exact check: exact E/B (FAST arithmetic, full bin range) on `count`
+// cells picked by a hash of the step, compared with the field values the
+// surrogate wrote (E_stat + KE e, B_stat + KMU b: the values the next step
+// uses).  stats[0] = max |dE|, [1] = max |E|, [2] = max |dB|, [3] = max |B|
+// (as float bits, atomicMax on non-negative floats), [4] = 1 when an exact
+// sample was non-finite
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t hash32(uint32_t x) {
     x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
     return x;
 }
 
+// |surrogate - exact| of one component.  Both finite: the difference.  Exactly
+// one finite: a huge error (forces the fallback).  Both non-finite: 0 -- a
+// non-finite source bin makes the exact sum non-finite in every cell, so the
+// exact kernel would write a non-finite field as well and the fallback could
+// not give a finite answer.
+__device__ __forceinline__ float sample_diff(float sur, float exact) {
+    const bool fs = isfinite(sur), fe = isfinite(exact);
+    if (fs && fe) return fabsf(sur - exact);
+    return fs == fe ? 0.0f : 3.0e38f;
+}
+
+// one warp per sampled cell: lanes take every 32nd bin, then a shuffle reduction
 __global__ void __launch_bounds__(128) k_sample_check(const DevLbm L, uint32_t count, uint32_t salt, uint32_t* stats,
                                                      const unsigned long long* counters) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count) return;
+    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (i >= count) return;  // warp-uniform
     salt += (uint32_t)counters[0] * 0x9e3779b9u;  // a new sample set every step, also under graph replay
     uint32_t n = hash32(i * 2654435761u + salt) % L.n;
     for (int tries = 0; tries < 8 && (L.flags[n] & F_BO) == F_S; tries++) n = hash32(n + 0x9e3779b9u) % L.n;
-    if ((L.flags[n] & F_BO) == F_S) return;
+    if ((L.flags[n] & F_BO) == F_S) return;  // warp-uniform
     uint32_t x, y, z;
     cell_xyz(L, n, x, y, z);
     const uint32_t own = x / L.bsx + (y / L.bsy + z / L.bsz * L.nd) * L.nd;
     float e[3] = {0, 0, 0}, b[3] = {0, 0, 0};
     const float4* qu = (const float4*)L.qu_lod;
-    for (uint32_t d = L.first_src; d < L.n_lod_own; d++) {
+    for (uint32_t d = L.first_src + lane; d < L.n_lod_own; d += 32u) {
         if (d == own) continue;
         const float4 p = L.lod_pos[d], v = qu[d];
         add_src<true>((float)x - p.x, (float)y - p.y, (float)z - p.z, make_float4(v.x, v.x * v.y, v.x * v.z, v.x * v.w),
                       e, b);
     }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            e[c] += __shfl_xor_sync(0xFFFFFFFFu, e[c], off);
+            b[c] += __shfl_xor_sync(0xFFFFFFFFu, b[c], off);
+        }
+    if (lane != 0) return;
     const size_t N = L.n;
     float dE = 0.0f, mE = 0.0f, dB = 0.0f, mB = 0.0f;
+    bool nonfinite = false;
     for (int c = 0; c < 3; c++) {
-        const float es = (L.e_dyn[c * N + n] - L.e_stat[c * N + n]) / L.ke;
-        const float bs = (L.b_dyn[c * N + n] - L.b_stat[c * N + n]) / L.kmu;
-        dE = fmaxf(dE, fabsf(es - e[c]));
-        mE = fmaxf(mE, fabsf(e[c]));
-        dB = fmaxf(dB, fabsf(bs - b[c]));
-        mB = fmaxf(mB, fabsf(b[c]));
+        const float ef = L.e_stat[c * N + n] + L.ke * e[c];
+        const float bf = L.b_stat[c * N + n] + L.kmu * b[c];
+        dE = fmaxf(dE, sample_diff(L.e_dyn[c * N + n], ef));
+        dB = fmaxf(dB, sample_diff(L.b_dyn[c * N + n], bf));
+        mE = fmaxf(mE, isfinite(ef) ? fabsf(ef) : 0.0f);
+        mB = fmaxf(mB, isfinite(bf) ? fabsf(bf) : 0.0f);
+        nonfinite |= !isfinite(ef) || !isfinite(bf);
     }
-    if (isnan(dE)) dE = 3.0e38f;
-    if (isnan(dB)) dB = 3.0e38f;
     atomicMax(&stats[0], __float_as_uint(dE));
     atomicMax(&stats[1], __float_as_uint(mE));
     atomicMax(&stats[2], __float_as_uint(dB));
     atomicMax(&stats[3], __float_as_uint(mB));
+    if (nonfinite) atomicOr(&stats[4], 1u);
 }
 
 // decides the fallback on the device: flag = 1 when a relative error exceeds tol
@@ -419,7 +568,8 @@ __global__ void k_sample_decide(uint32_t* stats, float tol, uint32_t* flag, floa
     last[1] = rB;
     counters[0] += 1ull;
     if (bad) counters[1] += 1ull;
-    stats[0] = stats[1] = stats[2] = stats[3] = 0u;
+    if (stats[4]) counters[2] += 1ull;
+    stats[0] = stats[1] = stats[2] = stats[3] = stats[4] = 0u;
 }
 
 // ---------------------------------------------------------------------------
@@ -428,7 +578,7 @@ __global__ void k_sample_decide(uint32_t* stats, float tol, uint32_t* flag, floa
 namespace {
 struct LayerDef { int cin, cout, dil; };
 const LayerDef kLayers[10] = {{4, 32, 1}, {32, 32, 1}, {32, 32, 2}, {32, 32, 2}, {32, 32, 4},
-                              {32, 32, 4}, {32, 32, 8}, {32, 32, 1}, {32, 32, 1}, {32, 48, 1}};
+                              {32, 32, 4}, {32, 32, 8}, {32, 32, 1}, {32, 32, 1}, {32, Surrogate::OUT_PAD, 1}};
 unsigned blocks_for(size_t n, unsigned b) { return (unsigned)((n + b - 1) / b); }
 }  // namespace
 
@@ -457,24 +607,31 @@ int Surrogate::init(int nd, float bsx, float bsy, float bsz, int first_src) {
         off += (size_t)kLayers[l].cin * kLayers[l].cout * 27;
     }
     nw_ = off;
+    off = 0;
+    for (int l = 0; l < 10; l++) {
+        wkoff_[l] = off;
+        off += (size_t)kLayers[l].cout * 27 * (kLayers[l].cin < 16 ? 16 : kLayers[l].cin);
+    }
+    nwk_ = off;
     int rc = 0;
     rc |= alloc((void**)&w_, nw_ * 4);
     rc |= alloc((void**)&gw_, nw_ * 4);
     rc |= alloc((void**)&m_, nw_ * 4);
     rc |= alloc((void**)&v_, nw_ * 4);
-    rc |= alloc((void**)&wt_, 32 * 48 * 27 * 4);
-    rc |= alloc((void**)&wk_, nw_ * 2);
+    rc |= alloc((void**)&wt_, (size_t)32 * OUT_PAD * 27 * 4);
+    rc |= alloc((void**)&wk_, nwk_ * 2);
     rc |= alloc((void**)&scales_, 4 * 4);
     rc |= alloc((void**)&stats_, 8 * 4);
     rc |= alloc((void**)&flag_, 4);
     rc |= alloc((void**)&last_, 2 * 4);
-    rc |= alloc((void**)&counters_, 2 * 8);
+    rc |= alloc((void**)&counters_, 3 * 8);
     rc |= alloc((void**)&xin_, (size_t)4 * V_ * 4);
-    rc |= alloc((void**)&yout_, (size_t)48 * V_ * 4);
+    rc |= alloc((void**)&yout_, (size_t)OUT_PAD * V_ * 4);
     rc |= alloc((void**)&ha_, (size_t)32 * V_ * 4);
     rc |= alloc((void**)&hb_, (size_t)32 * V_ * 4);
     rc |= alloc((void**)&ab_, (size_t)32 * V_ * 2);
     rc |= alloc((void**)&bb_, (size_t)32 * V_ * 2);
+    rc |= alloc((void**)&xb_, (size_t)16 * V_ * 2);
     if (rc) return ION_E_NOMEM;
     // He-style initialisation scaled down so the residual stack starts near identity
     std::mt19937 gen(12345);
@@ -489,12 +646,12 @@ int Surrogate::init(int nd, float bsx, float bsy, float bsz, int first_src) {
     return cudaGetLastError() == cudaSuccess ? ION_OK : ION_E_CUDA;
 }
 
-// FP32 forward of a batch; acts: 9 activation buffers [B][32][V] + output [B][48][V]
+// FP32 forward of a batch; acts: 9 activation buffers [B][32][V] + output [B][OUT_PAD][V]
 void Surrogate::forward_fp32(const float* X, int B, std::vector<float*>& acts, float* Y, cudaStream_t s) {
     auto conv = [&](const float* in, int l, const float* res, float* out) {
         const LayerDef& d = kLayers[l];
         dim3 grid(blocks_for((size_t)B * V_, 128), (d.cout + COG - 1) / COG);
-        k_conv_fwd<<<grid, 128, COG * d.cin * 27 * 4, s>>>(in, w_ + woff_[l], res, out, d.cin, d.cout, d.dil, nd_, B);
+        k_conv_fwd<<<grid, 128, 0, s>>>(in, w_ + woff_[l], res, out, d.cin, d.cout, d.dil, nd_, B);
     };
     // acts: h0, t0, h1, t1, h2, t2, h3, t3, h4
     conv(X, 0, nullptr, acts[0]);
@@ -516,7 +673,7 @@ void Surrogate::backward_fp32(const float* X, int B, std::vector<float*>& acts, 
         const LayerDef& d = kLayers[l];
         k_transpose_flip<<<blocks_for((size_t)d.cin * d.cout * 27, 256), 256, 0, s>>>(w_ + woff_[l], wt_, d.cin, d.cout);
         dim3 grid(blocks_for((size_t)B * V_, 128), (d.cin + COG - 1) / COG);
-        k_conv_fwd<<<grid, 128, COG * d.cout * 27 * 4, s>>>(gout, wt_, res, gin, d.cout, d.cin, d.dil, nd_, B);
+        k_conv_fwd<<<grid, 128, 0, s>>>(gout, wt_, res, gin, d.cout, d.cin, d.dil, nd_, B);
     };
     float* gh = g[0];
     float* gt = g[1];
@@ -538,7 +695,7 @@ void Surrogate::backward_fp32(const float* X, int B, std::vector<float*>& acts, 
 
 int Surrogate::train(int nsamples, int epochs, int batch, float lr, uint64_t seed, cudaStream_t s, float* rel_err) {
     // training snapshots: random charge and current per bin, exact far-field targets
-    const size_t xs = (size_t)4 * V_, ys = (size_t)48 * V_;
+    const size_t xs = (size_t)4 * V_, ys = (size_t)OUT_PAD * V_;
     float *X = nullptr, *T = nullptr;
     if (cudaMalloc(&X, xs * nsamples * 4) != cudaSuccess || cudaMalloc(&T, ys * nsamples * 4) != cudaSuccess) {
         cudaFree(X);
@@ -554,7 +711,8 @@ int Surrogate::train(int nsamples, int epochs, int batch, float lr, uint64_t see
                 for (int v = 0; v < V_; v++) h[sidx * xs + c * V_ + v] = v >= first_ ? U(gen) : 0.0f;
         cudaMemcpy(X, h.data(), h.size() * 4, cudaMemcpyHostToDevice);
     }
-    k_far_targets<<<blocks_for((size_t)V_ * 8 * nsamples, 256), 256, 0, s>>>(X, nd_, bs_[0], bs_[1], bs_[2], RNEAR, T,
+    cudaMemsetAsync(T, 0, ys * nsamples * 4, s);  // padding channels stay zero
+    k_far_targets<<<blocks_for((size_t)V_ * NODES * nsamples, 256), 256, 0, s>>>(X, nd_, bs_[0], bs_[1], bs_[2], RNEAR, T,
                                                                               nsamples);
     // normalisation of the E and B channel groups
     std::vector<float> th(ys * std::min(nsamples, 64));
@@ -563,28 +721,15 @@ int Surrogate::train(int nsamples, int epochs, int batch, float lr, uint64_t see
     double se = 0, sb = 0;
     size_t ne = 0, nb = 0;
     for (size_t i = 0; i < th.size(); i++) {
-        const int ch = (int)((i / V_) % 48) % 6;
-        if (ch < 3) { se += (double)th[i] * th[i]; ne++; } else { sb += (double)th[i] * th[i]; nb++; }
+        const int chan = (int)((i / V_) % OUT_PAD);
+        if (chan >= OUT_CH) continue;  // padding channels
+        if (chan % 6 < 3) { se += (double)th[i] * th[i]; ne++; } else { sb += (double)th[i] * th[i]; nb++; }
     }
     yE_ = (float)std::sqrt(se / std::max<size_t>(ne, 1));
     yB_ = (float)std::sqrt(sb / std::max<size_t>(nb, 1));
     if (!(yE_ > 0)) yE_ = 1.0f;
     if (!(yB_ > 0)) yB_ = 1.0f;
-    {
-        std::vector<float> scale(48 * (size_t)V_);
-        for (int ch = 0; ch < 48; ch++)
-            for (int v = 0; v < V_; v++) scale[(size_t)ch * V_ + v] = 1.0f / (ch % 6 < 3 ? yE_ : yB_);
-        float* d_scale = nullptr;
-        cudaMalloc(&d_scale, scale.size() * 4);
-        cudaMemcpy(d_scale, scale.data(), scale.size() * 4, cudaMemcpyHostToDevice);
-        // T *= scale per sample (elementwise with the per-sample pattern)
-        std::vector<float> all(ys * nsamples);
-        cudaMemcpy(all.data(), T, all.size() * 4, cudaMemcpyDeviceToHost);
-        for (int sidx = 0; sidx < nsamples; sidx++)
-            for (size_t i = 0; i < ys; i++) all[sidx * ys + i] *= scale[i];
-        cudaMemcpy(T, all.data(), all.size() * 4, cudaMemcpyHostToDevice);
-        cudaFree(d_scale);
-    }
+    k_scale_targets<<<blocks_for(ys * nsamples, 256), 256, 0, s>>>(T, V_, ys * nsamples, 1.0f / yE_, 1.0f / yB_);
     // activations and gradients for one batch
     std::vector<float*> acts(9), g(3);
     float *Yb = nullptr, *gY = nullptr, *loss = nullptr;
@@ -654,22 +799,26 @@ int Surrogate::train(int nsamples, int epochs, int batch, float lr, uint64_t see
 void Surrogate::pack_bf16(cudaStream_t s) {
     for (int l = 0; l < 10; l++) {
         const LayerDef& d = kLayers[l];
-        k_pack_weights<<<blocks_for((size_t)d.cin * d.cout * 27, 256), 256, 0, s>>>(w_ + woff_[l], wk_ + woff_[l], d.cin,
-                                                                                    d.cout);
+        const int cinp = d.cin < 16 ? 16 : d.cin;
+        k_pack_weights<<<blocks_for((size_t)d.cout * 27 * cinp, 256), 256, 0, s>>>(w_ + woff_[l], wk_ + wkoff_[l], d.cin,
+                                                                                    cinp, d.cout);
     }
 }
 
-// BF16 tensor-core forward of one sample X [4][V] (fp32) -> yout_ [48][V]
+// BF16 tensor-core forward of one sample X [4][V] (fp32) -> yout_ [OUT_PAD][V]
 void Surrogate::infer_bf16(const float* X, cudaStream_t s) {
-    // residual stream h in fp32 (ha_/hb_), bf16 copies for the next conv (ab_/bb_)
-    k_to_bf16<<<blocks_for((size_t)4 * V_, 256), 256, 0, s>>>(X, bb_, (size_t)4 * V_);
-    const unsigned grid = blocks_for((size_t)(V_ / 16) * 32, 128);
+    // residual stream h in fp32 (ha_/hb_), bf16 voxel-major copies for the next conv (xb_/ab_/bb_)
+    k_input_bf16<<<blocks_for((size_t)16 * V_, 256), 256, 0, s>>>(X, xb_, V_);
+    const unsigned gx = blocks_for((size_t)(V_ / 16) * 32, 128);
     auto conv = [&](const __nv_bfloat16* in, int l, const float* res, float* out, __nv_bfloat16* outb) {
         const LayerDef& d = kLayers[l];
-        if (d.cout == 32) k_conv_bf16<4><<<grid, 128, 0, s>>>(in, wk_ + woff_[l], res, out, outb, d.cin, d.dil, nd_);
-        else k_conv_bf16<6><<<grid, 128, 0, s>>>(in, wk_ + woff_[l], res, out, outb, d.cin, d.dil, nd_);
+        const __nv_bfloat16* wk = wk_ + wkoff_[l];
+        static_assert(OUT_PAD == 21 * 8, "head n-tiles");
+        if (l == 0) k_conv_bf16<16, 4><<<dim3(gx, 1), 128, 0, s>>>(in, wk, res, out, outb, d.cout, d.dil, nd_);
+        else if (d.cout == 32) k_conv_bf16<32, 4><<<dim3(gx, 1), 128, 0, s>>>(in, wk, res, out, outb, d.cout, d.dil, nd_);
+        else k_conv_bf16<32, 7><<<dim3(gx, 3), 128, 0, s>>>(in, wk, res, out, outb, d.cout, d.dil, nd_);
     };
-    conv(bb_, 0, nullptr, ha_, ab_);  // h0
+    conv(xb_, 0, nullptr, ha_, ab_);  // h0
     for (int i = 0; i < 4; i++) {
         conv(ab_, 1 + 2 * i, nullptr, hb_, bb_);  // t_i (fp32 copy unused)
         conv(bb_, 2 + 2 * i, ha_, ha_, ab_);      // h_{i+1} = h_i + conv(t_i)
@@ -681,8 +830,8 @@ void Surrogate::step(const DevLbm& L, cudaStream_t s, uint32_t salt) {
     k_source_scale<<<1, 256, 0, s>>>(L.qu_lod, V_, first_, scales_);
     k_pack_input_dev(L, s);
     infer_bf16(xin_, s);
-    k_surrogate_cells<<<blocks_for(L.n, 256), 256, 0, s>>>(L, yout_, scales_, yE_, yB_, RNEAR);
-    k_sample_check<<<blocks_for(check_cells_, 128), 128, 0, s>>>(L, check_cells_, salt, stats_, counters_);
+    k_surrogate_cells<<<L.n_bins, SC_THREADS, 0, s>>>(L, yout_, scales_, yE_, yB_);
+    k_sample_check<<<blocks_for((size_t)check_cells_ * 32, 128), 128, 0, s>>>(L, check_cells_, salt, stats_, counters_);
     k_sample_decide<<<1, 1, 0, s>>>(stats_, tol_, flag_, last_, counters_);
 }
 
@@ -718,7 +867,7 @@ int Surrogate::set_weights(const float* host, cudaStream_t s) {
 }
 
 int Surrogate::grad(const float* hX, const float* hT, int B, float* hloss, float* hgrad, cudaStream_t s) {
-    const size_t xs = (size_t)4 * V_, ys = (size_t)48 * V_;
+    const size_t xs = (size_t)4 * V_, ys = (size_t)OUT_PAD * V_;
     std::vector<float*> acts(9), g(3);
     float *X = nullptr, *T = nullptr, *Y = nullptr, *gY = nullptr, *loss = nullptr;
     bool ok = cudaMalloc(&X, xs * B * 4) == cudaSuccess && cudaMalloc(&T, ys * B * 4) == cudaSuccess &&
@@ -736,7 +885,8 @@ int Surrogate::grad(const float* hX, const float* hT, int B, float* hloss, float
         backward_fp32(X, B, acts, gY, g, s);
         cudaMemcpyAsync(hgrad, gw_, nw_ * 4, cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(hloss, loss, 4, cudaMemcpyDeviceToHost, s);
-        if (cudaStreamSynchronize(s) != cudaSuccess) rc = ION_E_CUDA;
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) rc = ION_E_CUDA;
+        *hloss /= (float)(ys * B);  // mean squared error, the loss whose gradient k_mse forms
     }
     for (auto p : acts) cudaFree(p);
     for (auto p : g) cudaFree(p);
@@ -745,8 +895,27 @@ int Surrogate::grad(const float* hX, const float* hT, int B, float* hloss, float
     return rc;
 }
 
+int Surrogate::targets(const float* hX, float* hT, int B, cudaStream_t s) {
+    const size_t xs = (size_t)4 * V_, ys = (size_t)OUT_PAD * V_;
+    float *X = nullptr, *T = nullptr;
+    int rc = cudaMalloc(&X, xs * B * 4) == cudaSuccess && cudaMalloc(&T, ys * B * 4) == cudaSuccess ? ION_OK
+                                                                                                  : ION_E_NOMEM;
+    if (!rc) {
+        cudaMemcpyAsync(X, hX, xs * B * 4, cudaMemcpyHostToDevice, s);
+        cudaMemsetAsync(T, 0, ys * B * 4, s);
+        k_far_targets<<<blocks_for((size_t)V_ * NODES * B, 256), 256, 0, s>>>(X, nd_, bs_[0], bs_[1], bs_[2], RNEAR, T,
+                                                                               B);
+        cudaMemcpyAsync(hT, T, ys * B * 4, cudaMemcpyDeviceToHost, s);
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) rc = ION_E_CUDA;
+    }
+    cudaFree(X);
+    cudaFree(T);
+    cudaGetLastError();
+    return rc;
+}
+
 int Surrogate::forward(const float* hX, float* hY, bool bf16, cudaStream_t s) {
-    const size_t xs = (size_t)4 * V_, ys = (size_t)48 * V_;
+    const size_t xs = (size_t)4 * V_, ys = (size_t)OUT_PAD * V_;
     std::vector<float*> acts(9);
     float *X = nullptr, *Y = nullptr;
     bool ok = cudaMalloc(&X, xs * 4) == cudaSuccess && cudaMalloc(&Y, ys * 4) == cudaSuccess;
@@ -761,7 +930,7 @@ int Surrogate::forward(const float* hX, float* hY, bool bf16, cudaStream_t s) {
             forward_fp32(X, 1, acts, Y, s);
             cudaMemcpyAsync(hY, Y, ys * 4, cudaMemcpyDeviceToHost, s);
         }
-        if (cudaStreamSynchronize(s) != cudaSuccess) rc = ION_E_CUDA;
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) rc = ION_E_CUDA;
     }
     for (auto p : acts) cudaFree(p);
     cudaFree(X); cudaFree(Y);
@@ -774,7 +943,7 @@ int Surrogate::save(const char* path) const {
     if (cudaMemcpy(w.data(), w_, nw_ * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return ION_E_CUDA;
     FILE* f = fopen(path, "wb");
     if (!f) return ION_E_IO;
-    const uint32_t hdr[4] = {0x474f5253u /* "SROG" */, 1u, (uint32_t)nd_, (uint32_t)nw_};
+    const uint32_t hdr[4] = {0x474f5253u /* "SROG" */, 2u, (uint32_t)nd_, (uint32_t)nw_};
     bool ok = fwrite(hdr, 4, 4, f) == 4 && fwrite(&yE_, 4, 1, f) == 1 && fwrite(&yB_, 4, 1, f) == 1 &&
               fwrite(w.data(), 4, nw_, f) == nw_;
     fclose(f);
@@ -786,7 +955,7 @@ int Surrogate::load(const char* path, cudaStream_t s) {
     if (!f) return ION_E_IO;
     uint32_t hdr[4];
     std::vector<float> w(nw_);
-    bool ok = fread(hdr, 4, 4, f) == 4 && hdr[0] == 0x474f5253u && hdr[1] == 1u && hdr[2] == (uint32_t)nd_ &&
+    bool ok = fread(hdr, 4, 4, f) == 4 && hdr[0] == 0x474f5253u && hdr[1] == 2u && hdr[2] == (uint32_t)nd_ &&
               hdr[3] == (uint32_t)nw_ && fread(&yE_, 4, 1, f) == 1 && fread(&yB_, 4, 1, f) == 1 &&
               fread(w.data(), 4, nw_, f) == nw_;
     fclose(f);

@@ -12,7 +12,11 @@ namespace ion {
 
 class Surrogate {
 public:
-    static constexpr int RNEAR = 2;  // bins within this Chebyshev distance are summed exactly
+    static constexpr int RNEAR = 2;           // bins within this Chebyshev distance are summed exactly
+    static constexpr int NODES = 27;          // 3 x 3 x 3 interpolation nodes per block
+    static constexpr int OUT_CH = NODES * 6;  // (Ex,Ey,Ez,Bx,By,Bz) per node
+    static constexpr int OUT_PAD = 168;       // head channels: OUT_CH rounded up to 8 (the rest are zero)
+    static constexpr int MAX_BLOCK = 64;      // largest LOD block edge (cells) the per-cell kernel tabulates
     ~Surrogate();
     int init(int nd, float bsx, float bsy, float bsz, int first_src);
     // generates `nsamples` snapshots (random charge/current per bin, exact far-field
@@ -26,10 +30,15 @@ public:
     uint32_t launches_per_step() const;
     bool ready() const { return ready_; }
     const uint32_t* fallback_flag() const { return flag_; }
-    void configure(float tol, uint32_t cells) { tol_ = tol; check_cells_ = cells; }
+    // tolerance and sample size of the check; restarts the statistics (and so the sample sequence)
+    void configure(float tol, uint32_t cells, cudaStream_t s) {
+        tol_ = tol;
+        check_cells_ = cells;
+        cudaMemsetAsync(counters_, 0, 3 * sizeof(unsigned long long), s);
+    }
     float tol() const { return tol_; }
     uint32_t check_cells() const { return check_cells_; }
-    // [0] checks, [1] fallbacks (device counters), [2..3] last relative errors
+    // counters: [0] checks, [1] fallbacks, [2] checks that saw a non-finite exact field; last: relative errors
     void stats_device(unsigned long long** counters, float** last) { *counters = counters_; *last = last_; }
     float rel32() const { return rel32_; }
     float rel16() const { return rel16_; }
@@ -40,6 +49,10 @@ public:
     int set_weights(const float* host, cudaStream_t s);
     // loss and weight gradient of one batch (host arrays; targets in the network's output scale)
     int grad(const float* hX, const float* hT, int B, float* loss, float* hgrad, cudaStream_t s);
+    // exact far-field targets (unscaled) of B source snapshots (host arrays)
+    int targets(const float* hX, float* hT, int B, cudaStream_t s);
+    float out_scale_e() const { return yE_; }
+    float out_scale_b() const { return yB_; }
     // FP32 (bf16=false) or BF16 tensor-core (bf16=true) forward of one sample (host arrays)
     int forward(const float* hX, float* hY, bool bf16, cudaStream_t s);
 
@@ -53,12 +66,12 @@ private:
 
     int nd_ = 0, V_ = 0, first_ = 0;
     float bs_[3] = {1, 1, 1};
-    size_t woff_[10] = {};
-    size_t nw_ = 0;
+    size_t woff_[10] = {}, wkoff_[10] = {};  // FP32 weights [co][ci][27]; packed BF16 [co][27][ci (>= 16)]
+    size_t nw_ = 0, nwk_ = 0;
     float *w_ = nullptr, *gw_ = nullptr, *m_ = nullptr, *v_ = nullptr, *wt_ = nullptr;
     __nv_bfloat16* wk_ = nullptr;
     float *scales_ = nullptr, *last_ = nullptr, *xin_ = nullptr, *yout_ = nullptr, *ha_ = nullptr, *hb_ = nullptr;
-    __nv_bfloat16 *ab_ = nullptr, *bb_ = nullptr;
+    __nv_bfloat16 *ab_ = nullptr, *bb_ = nullptr, *xb_ = nullptr;
     uint32_t *stats_ = nullptr, *flag_ = nullptr;
     unsigned long long* counters_ = nullptr;
     float yE_ = 1.0f, yB_ = 1.0f;

@@ -358,9 +358,18 @@ class Lbm:
         N.check(N.lib().ion_lbm_surrogate_configure(self._h, tolerance, check_cells))
 
     def surrogate_stats(self) -> dict:
-        c, f, e, b = C.c_uint64(), C.c_uint64(), C.c_float(), C.c_float()
-        N.check(N.lib().ion_lbm_surrogate_stats(self._h, C.byref(c), C.byref(f), C.byref(e), C.byref(b)))
-        return {"checks": c.value, "fallbacks": f.value, "err_e": e.value, "err_b": b.value}
+        c, f, nf, e, b = C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_float(), C.c_float()
+        N.check(N.lib().ion_lbm_surrogate_stats(self._h, C.byref(c), C.byref(f), C.byref(nf), C.byref(e), C.byref(b)))
+        return {"checks": c.value, "fallbacks": f.value, "nonfinite": nf.value, "err_e": e.value, "err_b": b.value}
+
+    def surrogate_targets(self, x: np.ndarray) -> tuple[np.ndarray, float, float]:
+        """Exact far-field targets of source snapshots x [S][4][V]; returns (t [S][168][V], yE, yB)."""
+        x = np.ascontiguousarray(x, np.float32)
+        S = x.shape[0]
+        t = np.empty((S, self.SURROGATE_OUT, x.shape[-1]), np.float32)
+        ye, yb = C.c_float(), C.c_float()
+        N.check(N.lib().ion_lbm_surrogate_targets(self._h, x.ctypes.data, t.ctypes.data, S, C.byref(ye), C.byref(yb)))
+        return t, ye.value, yb.value
 
     def surrogate_weights(self, values=None) -> np.ndarray:
         n = self._surrogate_count()
@@ -369,9 +378,11 @@ class Lbm:
         N.check(N.lib().ion_lbm_surrogate_weights(self._h, out.ctypes.data, None if src is None else src.ctypes.data, n))
         return out
 
+    SURROGATE_OUT = 168  # network output channels: 27 nodes x 6 components, padded to 168
+
     def _surrogate_count(self) -> int:
-        # layer table of the network (4->32, 8 x 32->32, 32->48; 3^3 kernels)
-        return (4 * 32 + 8 * 32 * 32 + 32 * 48) * 27
+        # layer table of the network (4->32, 8 x 32->32, 32->168; 3^3 kernels)
+        return (4 * 32 + 8 * 32 * 32 + 32 * self.SURROGATE_OUT) * 27
 
     def surrogate_grad(self, x: np.ndarray, t: np.ndarray) -> tuple[float, np.ndarray]:
         x = np.ascontiguousarray(x, np.float32)
@@ -385,7 +396,7 @@ class Lbm:
     def surrogate_forward(self, x: np.ndarray, bf16: bool = False) -> np.ndarray:
         x = np.ascontiguousarray(x, np.float32).reshape(-1)
         V = x.size // 4
-        y = np.empty(48 * V, np.float32)
+        y = np.empty(self.SURROGATE_OUT * V, np.float32)
         N.check(N.lib().ion_lbm_surrogate_forward(self._h, x.ctypes.data, y.ctypes.data, int(bf16)))
         return y
 
