@@ -59,7 +59,7 @@ FLOP_PER_INTERACTION = 34  # one source's E and B: 34 FLOP + 1 sqrt (sim_kernels
 # kernel-time results of one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum per launch);
 # the summaries with the commands that produced them are in profiles/
 NCU_TRAFFIC = {("tgv256", "k_stream_collide"): 2.506905e9, ("mhd128", "k_stream_collide"): 0.797089e9,
-               ("mhd128", "k_update_e_b<fast>"): 59.139e6}
+               ("mhd128", "k_update_e_b_fast"): 59.139e6}
 
 
 def parse():
@@ -510,7 +510,7 @@ def main():
         inter = sum(field_interactions(c["config"], d.read("flags")) for c, d in zip(cases, doms))
         if batch is None:
             avg = eb_ms / max(eb_n, 1)
-            kname = f"k_update_e_b<{a.field_mode}>"
+            kname = "k_update_e_b_exact" if a.field_mode == "bitwise" else "k_update_e_b_fast"
         else:
             avg = ms / a.steps
             kname = f"k_batch_step<{a.field_mode}> (whole step; FLOPs of its E/B phase)"

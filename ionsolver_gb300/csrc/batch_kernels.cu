@@ -7,7 +7,8 @@
 //   A  stream_collide of every cell of every domain   (sc_cell)
 //   B  LOD bin sums of every domain                     (lod_bin_warp)
 //   C  E/B update of every cell of every domain         (eb_tile)
-// Work is handed out in tiles of EB_CPT*blockDim cells (A, C) or one warp per bin
+// Work is handed out in tiles of EB_CPT*blockDim consecutive cells (A), bricks
+// or half bricks (C, as in the single-domain E/B kernel) or one warp per bin
 // (B); a tile's domain is found by binary search over prefix sums of the
 // per-domain tile counts.  Every cell runs exactly the per-cell code of the
 // single-domain kernels, so a batched step is bit-identical to stepping the
@@ -57,7 +58,7 @@ __device__ __forceinline__ bool grid_barrier(uint32_t* count, uint32_t* gen, uin
 
 template <int FT, bool MHD, bool FAST>
 __global__ void __launch_bounds__(256) k_batch_step(const BatchDev B, const uint32_t odd_t) {
-    __shared__ __align__(16) EbSmem sm;
+    __shared__ __align__(16) EbSmem<FAST> sm;
     __shared__ DevLbm sL;
     __shared__ uint32_t s_dom;
     const bool odd = odd_t != 0u;
@@ -94,14 +95,16 @@ __global__ void __launch_bounds__(256) k_batch_step(const BatchDev B, const uint
         // phase C: E/B update
         eb_init(sm);
         uint32_t uses[2] = {0u, 0u};
-        for (uint32_t t = blockIdx.x; t < B.total_tiles; t += nblocks) {
+        const uint32_t parts = 256u / blockDim.x;  // tiles per brick
+        for (uint32_t t = blockIdx.x; t < B.total_bricks; t += nblocks) {
             __syncthreads();
             if (threadIdx.x == 0) {
-                s_dom = find_domain(B.tile_off, B.ndom, t);
+                s_dom = find_domain(B.brick_off, B.ndom, t);
                 sL = B.doms[s_dom];
             }
             __syncthreads();
-            if (!eb_tile<FAST>(sL, (t - B.tile_off[s_dom]) * blockDim.x * EB_CPT, sm, uses)) {
+            const uint32_t local = t - B.brick_off[s_dom];
+            if (!eb_tile<FAST>(sL, local / parts, local % parts, sm, uses)) {
                 if (threadIdx.x == 0) atomicExch(B.err, 1u);
                 return;
             }

@@ -8,13 +8,13 @@ void launch_lod_bins(const DevLbm& L, cudaStream_t s) {
 }
 
 void launch_update_e_b_gated(const DevLbm& L, uint32_t* err, const uint32_t* gate, cudaStream_t s) {
-    k_update_e_b_gated<<<grid_for(L.n, 256 * EB_CPT), 256, 0, s>>>(L, err, gate);
+    k_update_e_b_gated<<<eb_bricks(L.nx, L.ny, L.nz), 256, 0, s>>>(L, err, gate);
 }
 
 void launch_update_e_b(const DevLbm& L, bool fast, uint32_t* err, cudaStream_t s) {
-    const unsigned g = grid_for(L.n, 256 * EB_CPT);
-    if (fast) k_update_e_b<true><<<g, 256, 0, s>>>(L, err);
-    else k_update_e_b<false><<<g, 256, 0, s>>>(L, err);
+    const unsigned g = eb_bricks(L.nx, L.ny, L.nz);
+    if (fast) k_update_e_b_fast<<<g, 256, 0, s>>>(L, err);
+    else k_update_e_b_exact<<<g, 256, 0, s>>>(L, err);
 }
 
 }  // namespace ion

@@ -213,6 +213,12 @@ __device__ __forceinline__ float2 sub2(float2 a, float2 b) {
         " mov.b64 {%0,%1}, rd;\n}" : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
     return d;
 }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+    float2 d;
+    asm("{.reg .b64 ra, rb, rd;\n mov.b64 ra, {%2,%3};\n mov.b64 rb, {%4,%5};\n add.rn.f32x2 rd, ra, rb;\n"
+        " mov.b64 {%0,%1}, rd;\n}" : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) {
     float2 d;
     asm("{.reg .b64 ra, rb, rd;\n mov.b64 ra, {%2,%3};\n mov.b64 rb, {%4,%5};\n mul.rn.f32x2 rd, ra, rb;\n"
@@ -227,47 +233,127 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
     return d;
 }
 
-// One FAST source, pre-broadcast into pairs for far_fast2:
-// (px,px,py,py) (pz,pz,q,q) (qvx,qvx,qvy,qvy) (qvz,qvz,wx,wx) (wy,wy,wz,wz)
+// FAST far field in coordinates relative to an origin o near the cells (the
+// centre of their brick): with c' = c - o and p' = p - o,
+//   |R|^2 = (|c'|^2 + |p'|^2) - 2 c'.p'                 (4 operations, no R)
+//   E = sum q R/|R|^3 = c' S - P,   S = sum q/|R|^3,  P = sum q p'/|R|^3
+//   B = sum qv x R/|R|^3 = A x c' - W,  A = sum qv/|R|^3,  W = sum (qv x p')/|R|^3
+// so one source costs 16 operations; |c'| is at most ~11 cells, which keeps
+// the expansion of |R|^2 and the split sums free of cancellation at the
+// distances that occur (the own bin is excluded).
+// One source, pre-broadcast into pairs for far_fast2 (m = -2 p'):
+// (mx,mx,my,my) (mz,mz,pp,pp) (q,q,qpx,qpx) (qpy,qpy,qpz,qpz) (qvx,qvx,qvy,qvy) (qvz,qvz,wx,wx) (wy,wy,wz,wz)
 struct FastSrc {
-    float4 d[5];
+    float4 d[7];
 };
 
-// far_fast for two cells at once (lanes .x and .y); same operations and
-// order per lane as far_fast.
+__device__ __forceinline__ void fast_src(FastSrc& f, float4 p, float4 v, float ox, float oy, float oz) {
+    // p = bin centre, v = (q, vx, vy, vz)
+    const float px = p.x - ox, py = p.y - oy, pz = p.z - oz;
+    const float pp = fmaf(pz, pz, fmaf(py, py, px * px));
+    const float q = v.x;
+    const float qx = q * v.y, qy = q * v.z, qz = q * v.w;
+    const float wx = qy * pz - qz * py, wy = qz * px - qx * pz, wz = qx * py - qy * px;
+    const float mx = -2.0f * px, my = -2.0f * py, mz = -2.0f * pz;
+    const float qpx = q * px, qpy = q * py, qpz = q * pz;
+    f.d[0] = make_float4(mx, mx, my, my);
+    f.d[1] = make_float4(mz, mz, pp, pp);
+    f.d[2] = make_float4(q, q, qpx, qpx);
+    f.d[3] = make_float4(qpy, qpy, qpz, qpz);
+    f.d[4] = make_float4(qx, qx, qy, qy);
+    f.d[5] = make_float4(qz, qz, wx, wx);
+    f.d[6] = make_float4(wy, wy, wz, wz);
+}
+
+// Far-field sums of two cells (lanes .x and .y) in relative coordinates.
 struct Pair3 {
     float2 x, y, z;
 };
-__device__ __forceinline__ void far_fast2(const Pair3& c, const FastSrc& S, Pair3& e, Pair3& A, Pair3& W) {
-    const float4 d0 = S.d[0], d1 = S.d[1], d2 = S.d[2], d3 = S.d[3], d4 = S.d[4];
-    const float2 rx = sub2(c.x, make_float2(d0.x, d0.y));
-    const float2 ry = sub2(c.y, make_float2(d0.z, d0.w));
-    const float2 rz = sub2(c.z, make_float2(d1.x, d1.y));
-    const float2 r2 = fma2(rz, rz, fma2(ry, ry, mul2(rx, rx)));
+struct FarSums {  // per cell pair: S, P, A, W
+    float2 S;
+    Pair3 P, A, W;
+};
+__device__ __forceinline__ void far_zero(FarSums& f) {
+    const float2 z = make_float2(0.0f, 0.0f);
+    f.S = z;
+    f.P = {z, z, z};
+    f.A = f.P;
+    f.W = f.P;
+}
+__device__ __forceinline__ void far_fast2(const Pair3& c, float2 cc, const FastSrc& S, FarSums& f) {
+    const float4 d0 = S.d[0], d1 = S.d[1], d2 = S.d[2], d3 = S.d[3], d4 = S.d[4], d5 = S.d[5], d6 = S.d[6];
+    float2 r2 = add2(cc, make_float2(d1.z, d1.w));
+    r2 = fma2(c.x, make_float2(d0.x, d0.y), r2);
+    r2 = fma2(c.y, make_float2(d0.z, d0.w), r2);
+    r2 = fma2(c.z, make_float2(d1.x, d1.y), r2);
     float2 inv;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(inv.x) : "f"(r2.x));
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(inv.y) : "f"(r2.y));
     const float2 inv3 = mul2(mul2(inv, inv), inv);
-    const float2 s = mul2(make_float2(d1.z, d1.w), inv3);
-    e.x = fma2(s, rx, e.x); e.y = fma2(s, ry, e.y); e.z = fma2(s, rz, e.z);
-    A.x = fma2(inv3, make_float2(d2.x, d2.y), A.x);
-    A.y = fma2(inv3, make_float2(d2.z, d2.w), A.y);
-    A.z = fma2(inv3, make_float2(d3.x, d3.y), A.z);
-    W.x = fma2(inv3, make_float2(d3.z, d3.w), W.x);
-    W.y = fma2(inv3, make_float2(d4.x, d4.y), W.y);
-    W.z = fma2(inv3, make_float2(d4.z, d4.w), W.z);
+    f.S = fma2(make_float2(d2.x, d2.y), inv3, f.S);
+    f.P.x = fma2(make_float2(d2.z, d2.w), inv3, f.P.x);
+    f.P.y = fma2(make_float2(d3.x, d3.y), inv3, f.P.y);
+    f.P.z = fma2(make_float2(d3.z, d3.w), inv3, f.P.z);
+    f.A.x = fma2(make_float2(d4.x, d4.y), inv3, f.A.x);
+    f.A.y = fma2(make_float2(d4.z, d4.w), inv3, f.A.y);
+    f.A.z = fma2(make_float2(d5.x, d5.y), inv3, f.A.z);
+    f.W.x = fma2(make_float2(d5.z, d5.w), inv3, f.W.x);
+    f.W.y = fma2(make_float2(d6.x, d6.y), inv3, f.W.y);
+    f.W.z = fma2(make_float2(d6.z, d6.w), inv3, f.W.z);
+}
+
+// far_fast2 for one lane (hi = false: .x, true: .y) -- the same operations
+// in the same order, for the source chunk that holds a cell's own bin
+__device__ __forceinline__ float& lane(float2& v, bool hi) { return hi ? v.y : v.x; }
+__device__ __forceinline__ void far_fast1(const Pair3& c, float2 cc, const FastSrc& S, FarSums& f, bool hi) {
+    const float4 d0 = S.d[0], d1 = S.d[1], d2 = S.d[2], d3 = S.d[3], d4 = S.d[4], d5 = S.d[5], d6 = S.d[6];
+    const float cx = hi ? c.x.y : c.x.x, cy = hi ? c.y.y : c.y.x, cz = hi ? c.z.y : c.z.x;
+    float r2 = (hi ? cc.y : cc.x) + d1.z;
+    r2 = fmaf(cx, d0.x, r2);
+    r2 = fmaf(cy, d0.z, r2);
+    r2 = fmaf(cz, d1.x, r2);
+    float inv;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
+    const float inv3 = (inv * inv) * inv;
+    lane(f.S, hi) = fmaf(d2.x, inv3, lane(f.S, hi));
+    lane(f.P.x, hi) = fmaf(d2.z, inv3, lane(f.P.x, hi));
+    lane(f.P.y, hi) = fmaf(d3.x, inv3, lane(f.P.y, hi));
+    lane(f.P.z, hi) = fmaf(d3.z, inv3, lane(f.P.z, hi));
+    lane(f.A.x, hi) = fmaf(d4.x, inv3, lane(f.A.x, hi));
+    lane(f.A.y, hi) = fmaf(d4.z, inv3, lane(f.A.y, hi));
+    lane(f.A.z, hi) = fmaf(d5.x, inv3, lane(f.A.z, hi));
+    lane(f.W.x, hi) = fmaf(d5.z, inv3, lane(f.W.x, hi));
+    lane(f.W.y, hi) = fmaf(d6.x, inv3, lane(f.W.y, hi));
+    lane(f.W.z, hi) = fmaf(d6.z, inv3, lane(f.W.z, hi));
+}
+
+// E and B of one lane from its far sums (relative coordinates c')
+__device__ __forceinline__ void far_finish(const Pair3& c, FarSums& f, bool hi, float* e, float* b) {
+    const float cx = hi ? c.x.y : c.x.x, cy = hi ? c.y.y : c.y.x, cz = hi ? c.z.y : c.z.x;
+    const float S = lane(f.S, hi);
+    const float Px = lane(f.P.x, hi), Py = lane(f.P.y, hi), Pz = lane(f.P.z, hi);
+    const float Ax = lane(f.A.x, hi), Ay = lane(f.A.y, hi), Az = lane(f.A.z, hi);
+    const float Wx = lane(f.W.x, hi), Wy = lane(f.W.y, hi), Wz = lane(f.W.z, hi);
+    e[0] = e[0] + (cx * S - Px);
+    e[1] = e[1] + (cy * S - Py);
+    e[2] = e[2] + (cz * S - Pz);
+    b[0] = b[0] + ((Ay * cz - Az * cy) - Wx);
+    b[1] = b[1] + ((Az * cx - Ax * cz) - Wy);
+    b[2] = b[2] + ((Ax * cy - Ay * cx) - Wz);
 }
 
 // Shared-memory staging area of one thread block; the mbarrier phase of each
 // buffer is tracked in `uses` so one block can process many tiles.
+template <bool FAST>
 struct EbSmem {
-    float4 pos[2][SRC_CHUNK];  // bin centres, as copied
-    float4 val[2][SRC_CHUNK];  // (q, vx, vy, vz), as copied
-    FastSrc fast[SRC_CHUNK];   // FAST: the chunk being summed, in pairs
+    float4 pos[2][SRC_CHUNK];          // bin centres, as copied
+    float4 val[2][SRC_CHUNK];          // (q, vx, vy, vz), as copied
+    FastSrc fast[FAST ? SRC_CHUNK : 1];  // FAST: the chunk being summed, in pairs
     uint64_t bar[2];
 };
 
-__device__ __forceinline__ void eb_init(EbSmem& sm) {
+template <class SM>
+__device__ __forceinline__ void eb_init(SM& sm) {
     if (threadIdx.x == 0) {
         mbar_init(&sm.bar[0], 1);
         mbar_init(&sm.bar[1], 1);
@@ -299,7 +385,8 @@ __device__ __forceinline__ void near_field(const DevLbm& L, uint32_t n, uint32_t
 }
 
 // Issues the bulk copies of source chunk c into buffer c & 1 (one thread).
-__device__ __forceinline__ void eb_issue(const DevLbm& L, EbSmem& sm, uint32_t c) {
+template <class SM>
+__device__ __forceinline__ void eb_issue(const DevLbm& L, SM& sm, uint32_t c) {
     const uint32_t first = L.first_src, last = L.n_lod_own;
     const uint32_t base = first + c * SRC_CHUNK;
     const uint32_t cnt = min(SRC_CHUNK, last - base);
@@ -319,41 +406,51 @@ __device__ __forceinline__ void eb_store(const DevLbm& L, uint32_t n, const floa
     L.b_dyn[2 * N + n] = L.b_stat[2 * N + n] + L.kmu * b[2];
 }
 
-// E/B of the cells [tile, tile + EB_CPT*blockDim.x) of domain L.  Returns
-// false (block-uniform) when a staged tile did not arrive within its wait
-// limit.  Per cell the sources are added in the reference's order; the
-// cell's own bin is skipped by a check that runs only in the one source
-// chunk that can contain it.  FAST holds the cells in pairs (2j, 2j+1) and
-// advances both with packed FP32 instructions.
+// E/B of the cells of one brick (or, with 128 threads, of half of one:
+// sub = 0, 1) of domain L.  Returns false (block-uniform) when a staged tile
+// did not arrive within its wait limit.  Per cell the sources are added in
+// the reference's order; the cell's own bin is skipped by a check that runs
+// only in the one source chunk that can contain it.  FAST holds the cells in
+// pairs (2j, 2j+1) and advances both with packed FP32 instructions.
 template <bool FAST>
-__device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t tile, EbSmem& sm, uint32_t (&uses)[2]) {
+__device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t brick, const uint32_t sub, EbSmem<FAST>& sm,
+                                        uint32_t (&uses)[2]) {
     static_assert(EB_CPT % 2 == 0, "cells are processed in pairs");
     constexpr uint32_t NP = EB_CPT / 2;
-    const uint32_t N = L.n;
+    const uint32_t nbx = (L.nx + EB_BX - 1) / EB_BX, nby = (L.ny + EB_BY - 1) / EB_BY;
+    const uint32_t bx = brick % nbx, by = (brick / nbx) % nby, bz = brick / (nbx * nby);
+    const uint32_t x = bx * EB_BX + threadIdx.x % EB_BX;
+    const uint32_t y = by * EB_BY + threadIdx.x / EB_BX + sub * (blockDim.x / EB_BX);
+    // brick centre: the origin of the FAST coordinates
+    const float ox = (float)(bx * EB_BX) + 0.5f * (float)(EB_BX - 1);
+    const float oy = (float)(by * EB_BY) + 0.5f * (float)(EB_BY - 1);
+    const float oz = (float)(bz * EB_CPT) + 0.5f * (float)(EB_CPT - 1);
     float e[EB_CPT][3], b[EB_CPT][3];  // near field (and, BITWISE, everything)
-    Pair3 cp[NP], pe[NP], pA[NP], pW[NP];  // FAST far field: coordinates, E, A = sum qv/r^3, W = sum (qv x p)/r^3
+    float ax[EB_CPT], ay[EB_CPT], az[EB_CPT];  // BITWISE: absolute coordinates
+    Pair3 cp[NP];                      // FAST: coordinates relative to the brick centre
+    float2 cc[NP];                     // FAST: |c'|^2
+    FarSums fs[NP];
     uint32_t own[EB_CPT];
     bool active[EB_CPT];
 #pragma unroll
     for (uint32_t k = 0; k < EB_CPT; k++) {
-        const uint32_t n = tile + threadIdx.x + k * blockDim.x;
-        active[k] = n < N && (L.flags[n] & F_BO) != F_S;
-        uint32_t x = 0, y = 0, z = 0;
-        if (n < N) cell_xyz(L, n, x, y, z);
+        const uint32_t z = bz * EB_CPT + k;
+        const bool inside = x < L.nx && y < L.ny && z < L.nz;
+        const uint32_t n = inside ? x + (y + z * L.ny) * L.nx : 0u;
+        active[k] = inside && (L.flags[n] & F_BO) != F_S;
         own[k] = active[k] ? x / L.bsx + (y / L.bsy + z / L.bsz * L.nd) * L.nd : 0xFFFFFFFFu;
-        const float fx = (float)x, fy = (float)y, fz = (float)z;
-        if (k & 1u) { cp[k / 2].x.y = fx; cp[k / 2].y.y = fy; cp[k / 2].z.y = fz; }
-        else { cp[k / 2].x.x = fx; cp[k / 2].y.x = fy; cp[k / 2].z.x = fz; }
+        ax[k] = (float)x; ay[k] = (float)y; az[k] = (float)z;
+        const float fx = (float)x - ox, fy = (float)y - oy, fz = (float)z - oz;
+        lane(cp[k / 2].x, k & 1u) = fx;
+        lane(cp[k / 2].y, k & 1u) = fy;
+        lane(cp[k / 2].z, k & 1u) = fz;
+        lane(cc[k / 2], k & 1u) = fmaf(fz, fz, fmaf(fy, fy, fx * fx));
 #pragma unroll
         for (int c = 0; c < 3; c++) { e[k][c] = 0.0f; b[k][c] = 0.0f; }
         if (active[k]) near_field<FAST>(L, n, x, y, z, e[k], b[k]);
     }
 #pragma unroll
-    for (uint32_t j = 0; j < NP; j++) {
-        pe[j] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-        pA[j] = pe[j];
-        pW[j] = pe[j];
-    }
+    for (uint32_t j = 0; j < NP; j++) far_zero(fs[j]);
 
     // depth-D LOD bins [first_src, n_lod_own) except the cell's own (sim_kernels.cl:940-955)
     const uint32_t first = L.first_src, last = L.n_lod_own;
@@ -375,57 +472,30 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t tile, Eb
         for (uint32_t k = 0; k < EB_CPT; k++) here |= (own[k] - base) < cnt;
         const bool any_own = __any_sync(0xFFFFFFFFu, here);  // this chunk holds some cell's own bin
         if constexpr (FAST) {
-            // per source: q v and q v x p, broadcast into pairs (once per chunk)
-            for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
-                const float4 p = sm.pos[buf][k], v = sm.val[buf][k];
-                const float qx = v.x * v.y, qy = v.x * v.z, qz = v.x * v.w;
-                const float wx = qy * p.z - qz * p.y, wy = qz * p.x - qx * p.z, wz = qx * p.y - qy * p.x;
-                FastSrc& f = sm.fast[k];
-                f.d[0] = make_float4(p.x, p.x, p.y, p.y);
-                f.d[1] = make_float4(p.z, p.z, v.x, v.x);
-                f.d[2] = make_float4(qx, qx, qy, qy);
-                f.d[3] = make_float4(qz, qz, wx, wx);
-                f.d[4] = make_float4(wy, wy, wz, wz);
-            }
+            for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x)
+                fast_src(sm.fast[k], sm.pos[buf][k], sm.val[buf][k], ox, oy, oz);
             __syncthreads();
-            const FastSrc* fs = sm.fast;
+            const FastSrc* src = sm.fast;
             if (any_own) {
                 for (uint32_t s = 0; s < cnt; s++) {
-                    const FastSrc S = fs[s];
+                    const FastSrc S = src[s];
 #pragma unroll
                     for (uint32_t j = 0; j < NP; j++) {
-                        if (base + s != own[2 * j] && base + s != own[2 * j + 1]) {
-                            far_fast2(cp[j], S, pe[j], pA[j], pW[j]);
+                        const bool lo_ok = base + s != own[2 * j], hi_ok = base + s != own[2 * j + 1];
+                        if (lo_ok && hi_ok) {
+                            far_fast2(cp[j], cc[j], S, fs[j]);
                         } else {  // one of the pair is in its own bin: scalar steps on the other
-                            const float4 p = make_float4(S.d[0].x, S.d[0].z, S.d[1].x, S.d[1].z);
-                            const float4 qv = make_float4(S.d[2].x, S.d[2].z, S.d[3].x, 0.0f);
-                            const float4 w = make_float4(S.d[3].z, S.d[4].x, S.d[4].z, 0.0f);
-                            const float4 pq = make_float4(p.x, p.y, p.z, S.d[1].z);
-                            if (base + s != own[2 * j]) {
-                                float ee[3] = {pe[j].x.x, pe[j].y.x, pe[j].z.x}, aa[3] = {pA[j].x.x, pA[j].y.x, pA[j].z.x},
-                                      ww[3] = {pW[j].x.x, pW[j].y.x, pW[j].z.x};
-                                far_fast(cp[j].x.x, cp[j].y.x, cp[j].z.x, pq, qv, w, ee, aa, ww);
-                                pe[j].x.x = ee[0]; pe[j].y.x = ee[1]; pe[j].z.x = ee[2];
-                                pA[j].x.x = aa[0]; pA[j].y.x = aa[1]; pA[j].z.x = aa[2];
-                                pW[j].x.x = ww[0]; pW[j].y.x = ww[1]; pW[j].z.x = ww[2];
-                            }
-                            if (base + s != own[2 * j + 1]) {
-                                float ee[3] = {pe[j].x.y, pe[j].y.y, pe[j].z.y}, aa[3] = {pA[j].x.y, pA[j].y.y, pA[j].z.y},
-                                      ww[3] = {pW[j].x.y, pW[j].y.y, pW[j].z.y};
-                                far_fast(cp[j].x.y, cp[j].y.y, cp[j].z.y, pq, qv, w, ee, aa, ww);
-                                pe[j].x.y = ee[0]; pe[j].y.y = ee[1]; pe[j].z.y = ee[2];
-                                pA[j].x.y = aa[0]; pA[j].y.y = aa[1]; pA[j].z.y = aa[2];
-                                pW[j].x.y = ww[0]; pW[j].y.y = ww[1]; pW[j].z.y = ww[2];
-                            }
+                            if (lo_ok) far_fast1(cp[j], cc[j], S, fs[j], false);
+                            if (hi_ok) far_fast1(cp[j], cc[j], S, fs[j], true);
                         }
                     }
                 }
             } else {
-#pragma unroll 2
+#pragma unroll 1
                 for (uint32_t s = 0; s < cnt; s++) {
-                    const FastSrc S = fs[s];
+                    const FastSrc S = src[s];
 #pragma unroll
-                    for (uint32_t j = 0; j < NP; j++) far_fast2(cp[j], S, pe[j], pA[j], pW[j]);
+                    for (uint32_t j = 0; j < NP; j++) far_fast2(cp[j], cc[j], S, fs[j]);
                 }
             }
         } else {
@@ -435,24 +505,15 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t tile, Eb
                 for (uint32_t s = 0; s < cnt; s++) {
                     const float4 p = sp[s], v = sv[s];
 #pragma unroll
-                    for (uint32_t k = 0; k < EB_CPT; k++) {
-                        const Pair3& q = cp[k / 2];
-                        const float fx = (k & 1u) ? q.x.y : q.x.x, fy = (k & 1u) ? q.y.y : q.y.x,
-                                    fz = (k & 1u) ? q.z.y : q.z.x;
-                        if (base + s != own[k]) add_src<false>(fx - p.x, fy - p.y, fz - p.z, v, e[k], b[k]);
-                    }
+                    for (uint32_t k = 0; k < EB_CPT; k++)
+                        if (base + s != own[k]) add_src<false>(ax[k] - p.x, ay[k] - p.y, az[k] - p.z, v, e[k], b[k]);
                 }
             } else {
 #pragma unroll 2
                 for (uint32_t s = 0; s < cnt; s++) {
                     const float4 p = sp[s], v = sv[s];
 #pragma unroll
-                    for (uint32_t k = 0; k < EB_CPT; k++) {
-                        const Pair3& q = cp[k / 2];
-                        const float fx = (k & 1u) ? q.x.y : q.x.x, fy = (k & 1u) ? q.y.y : q.y.x,
-                                    fz = (k & 1u) ? q.z.y : q.z.x;
-                        add_src<false>(fx - p.x, fy - p.y, fz - p.z, v, e[k], b[k]);
-                    }
+                    for (uint32_t k = 0; k < EB_CPT; k++) add_src<false>(ax[k] - p.x, ay[k] - p.y, az[k] - p.z, v, e[k], b[k]);
                 }
             }
         }
@@ -467,41 +528,34 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t tile, Eb
     }
 #pragma unroll
     for (uint32_t k = 0; k < EB_CPT; k++) {
-        const uint32_t n = tile + threadIdx.x + k * blockDim.x;
         if (!active[k]) continue;
-        if constexpr (FAST) {  // E = near part + far sum; B = near part + A x c - W
-            const uint32_t j = k / 2;
-            const bool hi = (k & 1u) != 0;
-            const float fx = hi ? cp[j].x.y : cp[j].x.x, fy = hi ? cp[j].y.y : cp[j].y.x, fz = hi ? cp[j].z.y : cp[j].z.x;
-            const float Ax = hi ? pA[j].x.y : pA[j].x.x, Ay = hi ? pA[j].y.y : pA[j].y.x, Az = hi ? pA[j].z.y : pA[j].z.x;
-            const float Wx = hi ? pW[j].x.y : pW[j].x.x, Wy = hi ? pW[j].y.y : pW[j].y.x, Wz = hi ? pW[j].z.y : pW[j].z.x;
-            e[k][0] = e[k][0] + (hi ? pe[j].x.y : pe[j].x.x);
-            e[k][1] = e[k][1] + (hi ? pe[j].y.y : pe[j].y.x);
-            e[k][2] = e[k][2] + (hi ? pe[j].z.y : pe[j].z.x);
-            b[k][0] = b[k][0] + ((Ay * fz - Az * fy) - Wx);
-            b[k][1] = b[k][1] + ((Az * fx - Ax * fz) - Wy);
-            b[k][2] = b[k][2] + ((Ax * fy - Ay * fx) - Wz);
-        }
-        eb_store(L, n, e[k], b[k]);
+        if constexpr (FAST) far_finish(cp[k / 2], fs[k / 2], (k & 1u) != 0, e[k], b[k]);
+        eb_store(L, x + (y + (bz * EB_CPT + k) * L.ny) * L.nx, e[k], b[k]);
     }
     return true;
 }
 
 // The exact update, run only when *gate != 0 (the surrogate's fallback decision)
-static __global__ void __launch_bounds__(256) k_update_e_b_gated(const DevLbm L, uint32_t* err, const uint32_t* gate) {
+static __global__ void __launch_bounds__(256, 2) k_update_e_b_gated(const DevLbm L, uint32_t* err, const uint32_t* gate) {
     if (*gate == 0u) return;
-    __shared__ __align__(16) EbSmem sm;
+    __shared__ __align__(16) EbSmem<true> sm;
     eb_init(sm);
     uint32_t uses[2] = {0u, 0u};
-    if (!eb_tile<true>(L, blockIdx.x * blockDim.x * EB_CPT, sm, uses) && threadIdx.x == 0) atomicExch(err, 1u);
+    if (!eb_tile<true>(L, blockIdx.x, 0u, sm, uses) && threadIdx.x == 0) atomicExch(err, 1u);
 }
 
-template <bool FAST>
-static __global__ void __launch_bounds__(256) k_update_e_b(const DevLbm L, uint32_t* err) {
-    __shared__ __align__(16) EbSmem sm;
+// FAST: 2 blocks of 256 threads per SM (registers); BITWISE: 3
+static __global__ void __launch_bounds__(256, 2) k_update_e_b_fast(const DevLbm L, uint32_t* err) {
+    __shared__ __align__(16) EbSmem<true> sm;
     eb_init(sm);
     uint32_t uses[2] = {0u, 0u};
-    if (!eb_tile<FAST>(L, blockIdx.x * blockDim.x * EB_CPT, sm, uses) && threadIdx.x == 0) atomicExch(err, 1u);
+    if (!eb_tile<true>(L, blockIdx.x, 0u, sm, uses) && threadIdx.x == 0) atomicExch(err, 1u);
+}
+static __global__ void __launch_bounds__(256, 3) k_update_e_b_exact(const DevLbm L, uint32_t* err) {
+    __shared__ __align__(16) EbSmem<false> sm;
+    eb_init(sm);
+    uint32_t uses[2] = {0u, 0u};
+    if (!eb_tile<false>(L, blockIdx.x, 0u, sm, uses) && threadIdx.x == 0) atomicExch(err, 1u);
 }
 
 }  // namespace ion

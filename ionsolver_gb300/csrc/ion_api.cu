@@ -1043,6 +1043,8 @@ struct ion_batch {
     DevLbm* d_doms = nullptr;
     uint32_t* d_tile_off[3] = {nullptr, nullptr, nullptr};  // block 128, 256, 512
     uint32_t total_tiles[3] = {0, 0, 0};
+    uint32_t* d_brick_off[3] = {nullptr, nullptr, nullptr};  // E/B tiles (bricks x 256 / block)
+    uint32_t total_bricks[3] = {0, 0, 0};
     uint32_t* d_bin_off = nullptr;
     uint32_t total_bins = 0;
     uint32_t* d_sync = nullptr;  // [0] barrier count, [1] barrier generation, [2] error
@@ -1069,6 +1071,8 @@ BatchDev batch_view(ion_batch* b, uint32_t block) {
     B.ndom = (uint32_t)b->doms.size();
     B.tile_off = b->d_tile_off[block_slot(block)];
     B.total_tiles = b->total_tiles[block_slot(block)];
+    B.brick_off = b->d_brick_off[block_slot(block)];
+    B.total_bricks = b->total_bricks[block_slot(block)];
     B.bin_off = b->d_bin_off;
     B.total_bins = b->total_bins;
     B.bar_count = b->d_sync;
@@ -1157,6 +1161,15 @@ int ion_batch_create(ion_lbm* const* domains, uint32_t count, ion_batch** out) {
         b->total_tiles[s] = tiles[count];
         rc = dalloc((void**)&b->d_tile_off[s], sizeof(uint32_t) * (count + 1));
         if (!rc && cudaMemcpy(b->d_tile_off[s], tiles.data(), sizeof(uint32_t) * (count + 1), cudaMemcpyHostToDevice) != cudaSuccess)
+            rc = fail(ION_E_CUDA, "batch table upload");
+        std::vector<uint32_t> bricks(count + 1, 0);
+        for (uint32_t i = 0; i < count; i++) {
+            const DevLbm& L = domains[i]->L;
+            bricks[i + 1] = bricks[i] + eb_bricks(L.nx, L.ny, L.nz) * (256u / kBatchBlocks[s]);
+        }
+        b->total_bricks[s] = bricks[count];
+        if (!rc) rc = dalloc((void**)&b->d_brick_off[s], sizeof(uint32_t) * (count + 1));
+        if (!rc && cudaMemcpy(b->d_brick_off[s], bricks.data(), sizeof(uint32_t) * (count + 1), cudaMemcpyHostToDevice) != cudaSuccess)
             rc = fail(ION_E_CUDA, "batch table upload");
     }
     if (!rc && (cudaMemcpy(b->d_doms, views.data(), sizeof(DevLbm) * count, cudaMemcpyHostToDevice) != cudaSuccess ||

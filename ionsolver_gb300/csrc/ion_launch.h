@@ -26,15 +26,26 @@ struct VoxArgs {
 constexpr unsigned RED_BLOCK = 256;
 
 // Cells per thread of the E/B update: each staged source is applied to
-// EB_CPT cells held in registers (cells tile + threadIdx.x + k*blockDim.x).
+// EB_CPT cells held in registers.
 constexpr uint32_t EB_CPT = 4;
+// The E/B update walks a domain in aligned bricks of EB_BX x EB_BY x EB_CPT
+// cells (1024 = 256 threads x EB_CPT); thread t of a 256-thread block holds
+// the cells (t % EB_BX, t / EB_BX, 0..EB_CPT-1) of its brick, a 128-thread
+// block one half of a brick (sub = 0, 1 in y).  FAST coordinates are taken
+// relative to the brick's centre, which depends only on the cell.
+constexpr uint32_t EB_BX = 16, EB_BY = 16;
+inline uint32_t eb_bricks(uint32_t nx, uint32_t ny, uint32_t nz) {
+    return ((nx + EB_BX - 1) / EB_BX) * ((ny + EB_BY - 1) / EB_BY) * ((nz + EB_CPT - 1) / EB_CPT);
+}
 
 // device view of a batch of domains (batch_kernels.cu)
 struct BatchDev {
     const DevLbm* doms;
     uint32_t ndom;
-    const uint32_t* tile_off;  // [ndom+1] prefix sums of ceil(n / blockDim)
+    const uint32_t* tile_off;  // [ndom+1] prefix sums of ceil(n / (EB_CPT * blockDim)) (stream_collide tiles)
     uint32_t total_tiles;
+    const uint32_t* brick_off;  // [ndom+1] prefix sums of bricks x (256 / blockDim) (E/B tiles)
+    uint32_t total_bricks;
     const uint32_t* bin_off;   // [ndom+1] prefix sums of n_lod_own
     uint32_t total_bins;
     uint32_t* bar_count;

@@ -132,6 +132,18 @@ __device__ __forceinline__ void ep_store(typename D::T* f, uint32_t N, uint32_t 
     }
 }
 
+// L2 prefetch of the slots ep_load will read (no registers held; the later
+// loads then wait on L2 instead of DRAM)
+template <class T, int Q, class NB>
+__device__ __forceinline__ void ep_prefetch(const T* f, uint32_t N, uint32_t n, bool odd, const NB& j) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(f + n));
+#pragma unroll
+    for (int i = 1; i < Q; i += 2) {
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(f + (size_t)(odd ? i : i + 1) * N + n));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(f + (size_t)(odd ? i + 1 : i) * N + j(i)));
+    }
+}
+
 template <class V>
 struct NbV {  // neighbour functor of a velocity set
     const Nbr& b;
@@ -265,6 +277,34 @@ __device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const
         cell_xyz(L, n, x, y, z);
         const Nbr nb(L, x, y, z);
         const NbV<V> j{nb};
+        const float w = L.w;
+        const float c_tau = fmaf(w, -0.5f, 1.0f);
+        // MHD: the electron gas first -- it reads no value of the gas lattice, so
+        // its DDFs are dead before the gas DDFs are loaded (same values, fewer
+        // registers live at once)
+        float rhoe = 0.0f, Bx = 0.0f, By = 0.0f, Bz = 0.0f, Ex = 0.0f, Ey = 0.0f, Ez = 0.0f;
+        if constexpr (MHD) {
+            // the gas and charge lattices are read after the electron gas: start them towards L2
+            ep_prefetch<T, Q>((const T*)L.fi, N, n, odd, j);
+            ep_prefetch<T, 7>((const T*)L.fqi, N, n, odd, Nb7{nb});
+            Bx = L.b_dyn[n]; By = L.b_dyn[(size_t)N + n]; Bz = L.b_dyn[2 * (size_t)N + n];
+            Ex = L.e_dyn[n]; Ey = L.e_dyn[(size_t)N + n]; Ez = L.e_dyn[2 * (size_t)N + n];
+            // electron gas: moments, Lorentz force, Guo half-step, SRT, store
+            float ehn[Q];
+            ep_load<D, Q>((const T*)L.ei, N, n, odd, j, ehn);
+            float uxe, uye, uze;
+            moments<V>(ehn, rhoe, uxe, uye, uze);
+            const float cxv = uye * Bz - uze * By, cyv = uze * Bx - uxe * Bz, czv = uxe * By - uye * Bx;
+            const float nre = -rhoe;
+            const float efx = nre * (Ex + cxv), efy = nre * (Ey + cyv), efz = nre * (Ez + czv);
+            const float r2e = 0.5f / (rhoe * L.kkge);
+            uxe = clampf(fmaf(efx, r2e, uxe), -CS, CS);
+            uye = clampf(fmaf(efy, r2e, uye), -CS, CS);
+            uze = clampf(fmaf(efz, r2e, uze), -CS, CS);
+            const ForceState fe = force_state<V>(uxe, uye, uze, efx, efy, efz);
+            const EqState ee = eq_state(rhoe, uxe, uye, uze);
+            srt_store<V, D>((T*)L.ei, N, n, odd, j, ehn, ee, fe, true, c_tau, w, eqc);
+        }
         float fhn[Q];
         ep_load<D, Q>((const T*)L.fi, N, n, odd, j, fhn);
         float rhon, uxn, uyn, uzn;
@@ -272,13 +312,9 @@ __device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const
         else moments<V>(fhn, rhon, uxn, uyn, uzn);
 
         float fxn = L.fx, fyn = L.fy, fzn = L.fz;
-        const float w = L.w;
-        const float c_tau = fmaf(w, -0.5f, 1.0f);
         if (L.ext_ff) { fxn = fxn + L.F[n]; fyn = fyn + L.F[(size_t)N + n]; fzn = fzn + L.F[2 * (size_t)N + n]; }
 
         if constexpr (MHD) {
-            const float Bx = L.b_dyn[n], By = L.b_dyn[(size_t)N + n], Bz = L.b_dyn[2 * (size_t)N + n];
-            const float Ex = L.e_dyn[n], Ey = L.e_dyn[(size_t)N + n], Ez = L.e_dyn[2 * (size_t)N + n];
             // charge advection (D3Q7): load, charge, collide, store
             const Nb7 j7{nb};
             float rhoq;
@@ -294,24 +330,6 @@ __device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const
 #pragma unroll
                 for (int i = 0; i < 7; i++) qhn[i] = fmaf(1.0f - L.wq, qhn[i], L.wq * aeq[i]);
                 ep_store<D, 7>((T*)L.fqi, N, n, odd, j7, qhn);
-            }
-            // electron gas: moments, Lorentz force, Guo half-step, SRT, store
-            float rhoe;
-            {
-                float ehn[Q];
-                ep_load<D, Q>((const T*)L.ei, N, n, odd, j, ehn);
-                float uxe, uye, uze;
-                moments<V>(ehn, rhoe, uxe, uye, uze);
-                const float cxv = uye * Bz - uze * By, cyv = uze * Bx - uxe * Bz, czv = uxe * By - uye * Bx;
-                const float nre = -rhoe;
-                const float efx = nre * (Ex + cxv), efy = nre * (Ey + cyv), efz = nre * (Ez + czv);
-                const float r2e = 0.5f / (rhoe * L.kkge);
-                uxe = clampf(fmaf(efx, r2e, uxe), -CS, CS);
-                uye = clampf(fmaf(efy, r2e, uye), -CS, CS);
-                uze = clampf(fmaf(efz, r2e, uze), -CS, CS);
-                const ForceState fe = force_state<V>(uxe, uye, uze, efx, efy, efz);
-                const EqState ee = eq_state(rhoe, uxe, uye, uze);
-                srt_store<V, D>((T*)L.ei, N, n, odd, j, ehn, ee, fe, true, c_tau, w, eqc);
             }
             L.q[n] = rhoq - rhoe;
             // Lorentz force on the gas

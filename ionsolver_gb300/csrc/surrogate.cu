@@ -376,16 +376,9 @@ __global__ void __launch_bounds__(SC_THREADS) k_surrogate_cells(const DevLbm L, 
             const bool ok = o < 125 && x >= 0 && y >= 0 && z >= 0 && x < nd && y < nd && z < nd && d != (int)bin &&
                             (uint32_t)d >= L.first_src;
             const uint32_t m = __ballot_sync(0xFFFFFFFFu, ok);
-            if (ok) {
-                const float4 p = L.lod_pos[d], v = qu[d];
-                const float qx = v.x * v.y, qy = v.x * v.z, qz = v.x * v.w;
-                const float wx = qy * p.z - qz * p.y, wy = qz * p.x - qx * p.z, wz = qx * p.y - qy * p.x;
-                FastSrc& f = sm.src[cnt + __popc(m & ((1u << lane) - 1u))];
-                f.d[0] = make_float4(p.x, p.x, p.y, p.y);
-                f.d[1] = make_float4(p.z, p.z, v.x, v.x);
-                f.d[2] = make_float4(qx, qx, qy, qy);
-                f.d[3] = make_float4(qz, qz, wx, wx);
-                f.d[4] = make_float4(wy, wy, wz, wz);
+            if (ok) {  // coordinates relative to this bin's centre
+                const float4 o = L.lod_pos[bin];
+                fast_src(sm.src[cnt + __popc(m & ((1u << lane) - 1u))], L.lod_pos[d], qu[d], o.x, o.y, o.z);
             }
             cnt += __popc(m);
         }
@@ -419,9 +412,12 @@ __device__ __forceinline__ void surrogate_tile(const DevLbm& L, const SurSmem& s
         lx = lc % L.bsx; ly = (lc / L.bsx) % L.bsy; lz = lc / (L.bsx * L.bsy);
         return li;
     };
-    Pair3 cp[SC_CPT / 2], pe[SC_CPT / 2], pA[SC_CPT / 2], pW[SC_CPT / 2];
+    Pair3 cp[SC_CPT / 2];  // cell coordinates relative to the bin centre
+    float2 cc[SC_CPT / 2];
+    FarSums fs[SC_CPT / 2];
     uint32_t live = 0u;  // bit k: cell k exists and is not solid
     const size_t N = L.n;
+    const float4 o = L.lod_pos[bin];
 #pragma unroll
     for (uint32_t k = 0; k < SC_CPT; k++) {
         uint32_t lx, ly, lz;
@@ -435,22 +431,20 @@ __device__ __forceinline__ void surrogate_tile(const DevLbm& L, const SurSmem& s
             asm volatile("prefetch.global.L2 [%0];" ::"l"(L.e_stat + c * N + m));
             asm volatile("prefetch.global.L2 [%0];" ::"l"(L.b_stat + c * N + m));
         }
-        float2& cx = cp[k / 2].x; float2& cy = cp[k / 2].y; float2& cz = cp[k / 2].z;
-        if (k & 1u) { cx.y = (float)x; cy.y = (float)y; cz.y = (float)z; }
-        else { cx.x = (float)x; cy.x = (float)y; cz.x = (float)z; }
+        const float fx = (float)x - o.x, fy = (float)y - o.y, fz = (float)z - o.z;
+        lane(cp[k / 2].x, k & 1u) = fx;
+        lane(cp[k / 2].y, k & 1u) = fy;
+        lane(cp[k / 2].z, k & 1u) = fz;
+        lane(cc[k / 2], k & 1u) = fmaf(fz, fz, fmaf(fy, fy, fx * fx));
     }
 #pragma unroll
-    for (uint32_t j = 0; j < SC_CPT / 2; j++) {
-        pe[j] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-        pA[j] = pe[j];
-        pW[j] = pe[j];
-    }
+    for (uint32_t j = 0; j < SC_CPT / 2; j++) far_zero(fs[j]);
     const uint32_t cnt = sm.count;
 #pragma unroll 1
     for (uint32_t s = 0; s < cnt; s++) {
         const FastSrc S = sm.src[s];
 #pragma unroll
-        for (uint32_t j = 0; j < SC_CPT / 2; j++) far_fast2(cp[j], S, pe[j], pA[j], pW[j]);
+        for (uint32_t j = 0; j < SC_CPT / 2; j++) far_fast2(cp[j], cc[j], S, fs[j]);
     }
 #pragma unroll
     for (uint32_t k = 0; k < SC_CPT; k++) {
@@ -458,13 +452,8 @@ __device__ __forceinline__ void surrogate_tile(const DevLbm& L, const SurSmem& s
         uint32_t lx, ly, lz;
         cell(k, lx, ly, lz);
         const uint32_t m = (bx * L.bsx + lx) + ((by * L.bsy + ly) + (bz * L.bsz + lz) * L.ny) * L.nx;
-        const uint32_t j = k / 2;
-        const bool hi = (k & 1u) != 0;
-        const float fx = hi ? cp[j].x.y : cp[j].x.x, fy = hi ? cp[j].y.y : cp[j].y.x, fz = hi ? cp[j].z.y : cp[j].z.x;
-        const float Ax = hi ? pA[j].x.y : pA[j].x.x, Ay = hi ? pA[j].y.y : pA[j].y.x, Az = hi ? pA[j].z.y : pA[j].z.x;
-        const float Wx = hi ? pW[j].x.y : pW[j].x.x, Wy = hi ? pW[j].y.y : pW[j].y.x, Wz = hi ? pW[j].z.y : pW[j].z.x;
-        const float e[3] = {hi ? pe[j].x.y : pe[j].x.x, hi ? pe[j].y.y : pe[j].y.x, hi ? pe[j].z.y : pe[j].z.x};
-        const float b[3] = {(Ay * fz - Az * fy) - Wx, (Az * fx - Ax * fz) - Wy, (Ax * fy - Ay * fx) - Wz};
+        float e[3] = {0.0f, 0.0f, 0.0f}, b[3] = {0.0f, 0.0f, 0.0f};
+        far_finish(cp[k / 2], fs[k / 2], (k & 1u) != 0, e, b);
         // triquadratic interpolation: the x contraction is tabulated per bin (t1)
         float wy[3], wz[3];
         quad_weights(L.bsy > 1 ? (float)ly / (float)(L.bsy - 1) : 0.0f, wy);
@@ -633,17 +622,20 @@ int Surrogate::init(int nd, float bsx, float bsy, float bsz, int first_src) {
     rc |= alloc((void**)&bb_, (size_t)32 * V_ * 2);
     rc |= alloc((void**)&xb_, (size_t)16 * V_ * 2);
     if (rc) return ION_E_NOMEM;
-    // He-style initialisation scaled down so the residual stack starts near identity
-    std::mt19937 gen(12345);
+    return reset_weights(seed_);
+}
+
+// He-style initialisation scaled down so the residual stack starts near identity
+int Surrogate::reset_weights(uint64_t seed) {
+    std::mt19937_64 gen(seed);
     std::vector<float> w(nw_);
     for (int l = 0; l < 10; l++) {
         const float sd = (l >= 1 && l <= 8 ? 0.1f : 1.0f) / std::sqrt((float)kLayers[l].cin * 27.0f);
         std::normal_distribution<float> nd1(0.0f, sd);
         for (size_t i = 0; i < (size_t)kLayers[l].cin * kLayers[l].cout * 27; i++) w[woff_[l] + i] = nd1(gen);
     }
-    cudaMemcpy(w_, w.data(), nw_ * 4, cudaMemcpyHostToDevice);
     ready_ = false;
-    return cudaGetLastError() == cudaSuccess ? ION_OK : ION_E_CUDA;
+    return cudaMemcpy(w_, w.data(), nw_ * 4, cudaMemcpyHostToDevice) == cudaSuccess ? ION_OK : ION_E_CUDA;
 }
 
 // FP32 forward of a batch; acts: 9 activation buffers [B][32][V] + output [B][OUT_PAD][V]
@@ -694,6 +686,8 @@ void Surrogate::backward_fp32(const float* X, int B, std::vector<float*>& acts, 
 }
 
 int Surrogate::train(int nsamples, int epochs, int batch, float lr, uint64_t seed, cudaStream_t s, float* rel_err) {
+    // every training starts from the same initial weights (a function of the seed)
+    if (int rc = reset_weights(seed ^ 0x5EEDu)) return rc;
     // training snapshots: random charge and current per bin, exact far-field targets
     const size_t xs = (size_t)4 * V_, ys = (size_t)OUT_PAD * V_;
     float *X = nullptr, *T = nullptr;
@@ -746,8 +740,16 @@ int Surrogate::train(int nsamples, int epochs, int batch, float lr, uint64_t see
     cudaMemsetAsync(m_, 0, nw_ * 4, s);
     cudaMemsetAsync(v_, 0, nw_ * 4, s);
     loss_.clear();
+    // divergence guard: the weights of the best epoch are kept; an epoch whose
+    // loss is not finite or above 4x the best restores them, clears the Adam
+    // moments and halves the learning rate from then on
+    float* wbest = nullptr;
+    if (!rc && cudaMalloc(&wbest, nw_ * 4) != cudaSuccess) rc = ION_E_NOMEM;
+    if (!rc) cudaMemcpyAsync(wbest, w_, nw_ * 4, cudaMemcpyDeviceToDevice, s);
+    double best = 1e300;
+    float lr_scale = 1.0f;
     for (int ep = 0; ep < epochs && !rc; ep++) {
-        const float lr_ep = lr * (ep < epochs / 2 ? 1.0f : ep < 3 * epochs / 4 ? 0.3f : 0.1f);
+        const float lr_ep = lr_scale * lr * (ep < epochs / 2 ? 1.0f : ep < 3 * epochs / 4 ? 0.3f : 0.1f);
         double ep_loss = 0.0;
         int nb_ = 0;
         for (int b0 = 0; b0 + batch <= ntrain; b0 += batch) {
@@ -764,9 +766,21 @@ int Surrogate::train(int nsamples, int epochs, int batch, float lr, uint64_t see
             ep_loss += lh / ((double)batch * ys);
             nb_++;
         }
-        loss_.push_back((float)(ep_loss / std::max(nb_, 1)));
+        const double el = ep_loss / std::max(nb_, 1);
+        loss_.push_back((float)el);
         if (cudaGetLastError() != cudaSuccess) rc = ION_E_CUDA;
+        if (std::isfinite(el) && el < best) {
+            best = el;
+            cudaMemcpyAsync(wbest, w_, nw_ * 4, cudaMemcpyDeviceToDevice, s);
+        } else if (!std::isfinite(el) || el > 4.0 * best) {
+            cudaMemcpyAsync(w_, wbest, nw_ * 4, cudaMemcpyDeviceToDevice, s);
+            cudaMemsetAsync(m_, 0, nw_ * 4, s);
+            cudaMemsetAsync(v_, 0, nw_ * 4, s);
+            lr_scale *= 0.5f;
+        }
     }
+    if (!rc && !(loss_.empty()) && !(loss_.back() <= best)) cudaMemcpyAsync(w_, wbest, nw_ * 4, cudaMemcpyDeviceToDevice, s);
+    cudaFree(wbest);
     // held-out error of the FP32 network and of the BF16 inference path
     if (!rc) {
         pack_bf16(s);

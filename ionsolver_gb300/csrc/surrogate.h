@@ -58,6 +58,7 @@ public:
 
 private:
     int alloc(void** p, size_t bytes);
+    int reset_weights(uint64_t seed);
     void forward_fp32(const float* X, int B, std::vector<float*>& acts, float* Y, cudaStream_t s);
     void backward_fp32(const float* X, int B, std::vector<float*>& acts, const float* gY, std::vector<float*>& g,
                        cudaStream_t s);
@@ -79,6 +80,7 @@ private:
     uint32_t check_cells_ = 1024;
     float rel32_ = -1.0f, rel16_ = -1.0f;
     bool ready_ = false;
+    uint64_t seed_ = 12345;
     std::vector<float> loss_;
     std::vector<void*> allocs_;
 };
