@@ -203,33 +203,43 @@ __device__ __forceinline__ void far_fast(float cx, float cy, float cz, float4 p,
     W[0] = fmaf(inv3, w.x, W[0]); W[1] = fmaf(inv3, w.y, W[1]); W[2] = fmaf(inv3, w.z, W[2]);
 }
 
-// Packed FP32 pairs (PTX add/sub/mul/fma .f32x2, sm_100 and later): one
-// instruction does the same IEEE round-to-nearest operation on two lanes of
-// data, so two cells advance through one source with half the issue slots
-// and bit for bit the values of the scalar code.
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
-    float2 d;
-    asm("{.reg .b64 ra, rb, rd;\n mov.b64 ra, {%2,%3};\n mov.b64 rb, {%4,%5};\n sub.rn.f32x2 rd, ra, rb;\n"
-        " mov.b64 {%0,%1}, rd;\n}" : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+// Packed FP32 pairs (PTX add/mul/fma .f32x2, sm_100 and later): one
+// instruction does the same IEEE round-to-nearest operation on the two
+// halves of a 64-bit register, so two cells advance through one source with
+// half the issue slots and bit for bit the values of the scalar code.  A pair
+// lives in a 64-bit integer (low half = first cell) from load to store, so no
+// packing moves are needed between the instructions.
+using P2 = unsigned long long;
+__device__ __forceinline__ P2 pk(float lo, float hi) {
+    P2 r;
+    asm("mov.b64 %0, {%1,%2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float lo32(P2 v) {
+    float a, b;
+    asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+    return a;
+}
+__device__ __forceinline__ float hi32(P2 v) {
+    float a, b;
+    asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+    return b;
+}
+__device__ __forceinline__ float half(P2 v, bool hi) { return hi ? hi32(v) : lo32(v); }
+__device__ __forceinline__ void set_half(P2& v, bool hi, float x) { v = hi ? pk(lo32(v), x) : pk(x, hi32(v)); }
+__device__ __forceinline__ P2 add2(P2 a, P2 b) {
+    P2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
     return d;
 }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) {
-    float2 d;
-    asm("{.reg .b64 ra, rb, rd;\n mov.b64 ra, {%2,%3};\n mov.b64 rb, {%4,%5};\n add.rn.f32x2 rd, ra, rb;\n"
-        " mov.b64 {%0,%1}, rd;\n}" : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+__device__ __forceinline__ P2 mul2(P2 a, P2 b) {
+    P2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
     return d;
 }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
-    float2 d;
-    asm("{.reg .b64 ra, rb, rd;\n mov.b64 ra, {%2,%3};\n mov.b64 rb, {%4,%5};\n mul.rn.f32x2 rd, ra, rb;\n"
-        " mov.b64 {%0,%1}, rd;\n}" : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return d;
-}
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
-    float2 d;
-    asm("{.reg .b64 ra, rb, rc, rd;\n mov.b64 ra, {%2,%3};\n mov.b64 rb, {%4,%5};\n mov.b64 rc, {%6,%7};\n"
-        " fma.rn.f32x2 rd, ra, rb, rc;\n mov.b64 {%0,%1}, rd;\n}"
-        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+__device__ __forceinline__ P2 fma2(P2 a, P2 b, P2 c) {
+    P2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
     return d;
 }
 
@@ -265,75 +275,74 @@ __device__ __forceinline__ void fast_src(FastSrc& f, float4 p, float4 v, float o
     f.d[6] = make_float4(wy, wy, wz, wz);
 }
 
-// Far-field sums of two cells (lanes .x and .y) in relative coordinates.
+// Far-field sums of two cells (the two halves of every pair).
 struct Pair3 {
-    float2 x, y, z;
+    P2 x, y, z;
 };
 struct FarSums {  // per cell pair: S, P, A, W
-    float2 S;
+    P2 S;
     Pair3 P, A, W;
 };
 __device__ __forceinline__ void far_zero(FarSums& f) {
-    const float2 z = make_float2(0.0f, 0.0f);
-    f.S = z;
-    f.P = {z, z, z};
+    f.S = 0ull;
+    f.P = {0ull, 0ull, 0ull};
     f.A = f.P;
     f.W = f.P;
 }
-__device__ __forceinline__ void far_fast2(const Pair3& c, float2 cc, const FastSrc& S, FarSums& f) {
-    const float4 d0 = S.d[0], d1 = S.d[1], d2 = S.d[2], d3 = S.d[3], d4 = S.d[4], d5 = S.d[5], d6 = S.d[6];
-    float2 r2 = add2(cc, make_float2(d1.z, d1.w));
-    r2 = fma2(c.x, make_float2(d0.x, d0.y), r2);
-    r2 = fma2(c.y, make_float2(d0.z, d0.w), r2);
-    r2 = fma2(c.z, make_float2(d1.x, d1.y), r2);
-    float2 inv;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(inv.x) : "f"(r2.x));
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(inv.y) : "f"(r2.y));
-    const float2 inv3 = mul2(mul2(inv, inv), inv);
-    f.S = fma2(make_float2(d2.x, d2.y), inv3, f.S);
-    f.P.x = fma2(make_float2(d2.z, d2.w), inv3, f.P.x);
-    f.P.y = fma2(make_float2(d3.x, d3.y), inv3, f.P.y);
-    f.P.z = fma2(make_float2(d3.z, d3.w), inv3, f.P.z);
-    f.A.x = fma2(make_float2(d4.x, d4.y), inv3, f.A.x);
-    f.A.y = fma2(make_float2(d4.z, d4.w), inv3, f.A.y);
-    f.A.z = fma2(make_float2(d5.x, d5.y), inv3, f.A.z);
-    f.W.x = fma2(make_float2(d5.z, d5.w), inv3, f.W.x);
-    f.W.y = fma2(make_float2(d6.x, d6.y), inv3, f.W.y);
-    f.W.z = fma2(make_float2(d6.z, d6.w), inv3, f.W.z);
+__device__ __forceinline__ void far_fast2(const Pair3& c, P2 cc, const FastSrc& src, FarSums& f) {
+    const ulonglong2* u = reinterpret_cast<const ulonglong2*>(src.d);
+    const ulonglong2 d0 = u[0], d1 = u[1], d2 = u[2], d3 = u[3], d4 = u[4], d5 = u[5], d6 = u[6];
+    P2 r2 = add2(cc, d1.y);
+    r2 = fma2(c.x, d0.x, r2);
+    r2 = fma2(c.y, d0.y, r2);
+    r2 = fma2(c.z, d1.x, r2);
+    float i0, i1;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(i0) : "f"(lo32(r2)));
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(i1) : "f"(hi32(r2)));
+    const P2 inv = pk(i0, i1);
+    const P2 inv3 = mul2(mul2(inv, inv), inv);
+    f.S = fma2(d2.x, inv3, f.S);
+    f.P.x = fma2(d2.y, inv3, f.P.x);
+    f.P.y = fma2(d3.x, inv3, f.P.y);
+    f.P.z = fma2(d3.y, inv3, f.P.z);
+    f.A.x = fma2(d4.x, inv3, f.A.x);
+    f.A.y = fma2(d4.y, inv3, f.A.y);
+    f.A.z = fma2(d5.x, inv3, f.A.z);
+    f.W.x = fma2(d5.y, inv3, f.W.x);
+    f.W.y = fma2(d6.x, inv3, f.W.y);
+    f.W.z = fma2(d6.y, inv3, f.W.z);
 }
 
-// far_fast2 for one lane (hi = false: .x, true: .y) -- the same operations
-// in the same order, for the source chunk that holds a cell's own bin
-__device__ __forceinline__ float& lane(float2& v, bool hi) { return hi ? v.y : v.x; }
-__device__ __forceinline__ void far_fast1(const Pair3& c, float2 cc, const FastSrc& S, FarSums& f, bool hi) {
+// far_fast2 for one half (hi = false: first cell, true: second) -- the same
+// operations in the same order, for the source chunk that holds a cell's own bin
+__device__ __forceinline__ void far_fast1(const Pair3& c, P2 cc, const FastSrc& S, FarSums& f, bool hi) {
     const float4 d0 = S.d[0], d1 = S.d[1], d2 = S.d[2], d3 = S.d[3], d4 = S.d[4], d5 = S.d[5], d6 = S.d[6];
-    const float cx = hi ? c.x.y : c.x.x, cy = hi ? c.y.y : c.y.x, cz = hi ? c.z.y : c.z.x;
-    float r2 = (hi ? cc.y : cc.x) + d1.z;
-    r2 = fmaf(cx, d0.x, r2);
-    r2 = fmaf(cy, d0.z, r2);
-    r2 = fmaf(cz, d1.x, r2);
+    float r2 = half(cc, hi) + d1.z;
+    r2 = fmaf(half(c.x, hi), d0.x, r2);
+    r2 = fmaf(half(c.y, hi), d0.z, r2);
+    r2 = fmaf(half(c.z, hi), d1.x, r2);
     float inv;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
     const float inv3 = (inv * inv) * inv;
-    lane(f.S, hi) = fmaf(d2.x, inv3, lane(f.S, hi));
-    lane(f.P.x, hi) = fmaf(d2.z, inv3, lane(f.P.x, hi));
-    lane(f.P.y, hi) = fmaf(d3.x, inv3, lane(f.P.y, hi));
-    lane(f.P.z, hi) = fmaf(d3.z, inv3, lane(f.P.z, hi));
-    lane(f.A.x, hi) = fmaf(d4.x, inv3, lane(f.A.x, hi));
-    lane(f.A.y, hi) = fmaf(d4.z, inv3, lane(f.A.y, hi));
-    lane(f.A.z, hi) = fmaf(d5.x, inv3, lane(f.A.z, hi));
-    lane(f.W.x, hi) = fmaf(d5.z, inv3, lane(f.W.x, hi));
-    lane(f.W.y, hi) = fmaf(d6.x, inv3, lane(f.W.y, hi));
-    lane(f.W.z, hi) = fmaf(d6.z, inv3, lane(f.W.z, hi));
+    set_half(f.S, hi, fmaf(d2.x, inv3, half(f.S, hi)));
+    set_half(f.P.x, hi, fmaf(d2.z, inv3, half(f.P.x, hi)));
+    set_half(f.P.y, hi, fmaf(d3.x, inv3, half(f.P.y, hi)));
+    set_half(f.P.z, hi, fmaf(d3.z, inv3, half(f.P.z, hi)));
+    set_half(f.A.x, hi, fmaf(d4.x, inv3, half(f.A.x, hi)));
+    set_half(f.A.y, hi, fmaf(d4.z, inv3, half(f.A.y, hi)));
+    set_half(f.A.z, hi, fmaf(d5.x, inv3, half(f.A.z, hi)));
+    set_half(f.W.x, hi, fmaf(d5.z, inv3, half(f.W.x, hi)));
+    set_half(f.W.y, hi, fmaf(d6.x, inv3, half(f.W.y, hi)));
+    set_half(f.W.z, hi, fmaf(d6.z, inv3, half(f.W.z, hi)));
 }
 
-// E and B of one lane from its far sums (relative coordinates c')
-__device__ __forceinline__ void far_finish(const Pair3& c, FarSums& f, bool hi, float* e, float* b) {
-    const float cx = hi ? c.x.y : c.x.x, cy = hi ? c.y.y : c.y.x, cz = hi ? c.z.y : c.z.x;
-    const float S = lane(f.S, hi);
-    const float Px = lane(f.P.x, hi), Py = lane(f.P.y, hi), Pz = lane(f.P.z, hi);
-    const float Ax = lane(f.A.x, hi), Ay = lane(f.A.y, hi), Az = lane(f.A.z, hi);
-    const float Wx = lane(f.W.x, hi), Wy = lane(f.W.y, hi), Wz = lane(f.W.z, hi);
+// E and B of one half from its far sums (relative coordinates c')
+__device__ __forceinline__ void far_finish(const Pair3& c, const FarSums& f, bool hi, float* e, float* b) {
+    const float cx = half(c.x, hi), cy = half(c.y, hi), cz = half(c.z, hi);
+    const float S = half(f.S, hi);
+    const float Px = half(f.P.x, hi), Py = half(f.P.y, hi), Pz = half(f.P.z, hi);
+    const float Ax = half(f.A.x, hi), Ay = half(f.A.y, hi), Az = half(f.A.z, hi);
+    const float Wx = half(f.W.x, hi), Wy = half(f.W.y, hi), Wz = half(f.W.z, hi);
     e[0] = e[0] + (cx * S - Px);
     e[1] = e[1] + (cy * S - Py);
     e[2] = e[2] + (cz * S - Pz);
@@ -427,8 +436,7 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t brick, c
     const float oz = (float)(bz * EB_CPT) + 0.5f * (float)(EB_CPT - 1);
     float e[EB_CPT][3], b[EB_CPT][3];  // near field (and, BITWISE, everything)
     float ax[EB_CPT], ay[EB_CPT], az[EB_CPT];  // BITWISE: absolute coordinates
-    Pair3 cp[NP];                      // FAST: coordinates relative to the brick centre
-    float2 cc[NP];                     // FAST: |c'|^2
+    float rx[EB_CPT], ry[EB_CPT], rz[EB_CPT];  // FAST: coordinates relative to the brick centre
     FarSums fs[NP];
     uint32_t own[EB_CPT];
     bool active[EB_CPT];
@@ -440,17 +448,20 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t brick, c
         active[k] = inside && (L.flags[n] & F_BO) != F_S;
         own[k] = active[k] ? x / L.bsx + (y / L.bsy + z / L.bsz * L.nd) * L.nd : 0xFFFFFFFFu;
         ax[k] = (float)x; ay[k] = (float)y; az[k] = (float)z;
-        const float fx = (float)x - ox, fy = (float)y - oy, fz = (float)z - oz;
-        lane(cp[k / 2].x, k & 1u) = fx;
-        lane(cp[k / 2].y, k & 1u) = fy;
-        lane(cp[k / 2].z, k & 1u) = fz;
-        lane(cc[k / 2], k & 1u) = fmaf(fz, fz, fmaf(fy, fy, fx * fx));
+        rx[k] = (float)x - ox; ry[k] = (float)y - oy; rz[k] = (float)z - oz;
 #pragma unroll
         for (int c = 0; c < 3; c++) { e[k][c] = 0.0f; b[k][c] = 0.0f; }
         if (active[k]) near_field<FAST>(L, n, x, y, z, e[k], b[k]);
     }
+    Pair3 cp[NP];  // FAST: the relative coordinates in pairs, and |c'|^2
+    P2 cc[NP];
 #pragma unroll
-    for (uint32_t j = 0; j < NP; j++) far_zero(fs[j]);
+    for (uint32_t j = 0; j < NP; j++) {
+        cp[j] = {pk(rx[2 * j], rx[2 * j + 1]), pk(ry[2 * j], ry[2 * j + 1]), pk(rz[2 * j], rz[2 * j + 1])};
+        cc[j] = pk(fmaf(rz[2 * j], rz[2 * j], fmaf(ry[2 * j], ry[2 * j], rx[2 * j] * rx[2 * j])),
+                   fmaf(rz[2 * j + 1], rz[2 * j + 1], fmaf(ry[2 * j + 1], ry[2 * j + 1], rx[2 * j + 1] * rx[2 * j + 1])));
+        far_zero(fs[j]);
+    }
 
     // depth-D LOD bins [first_src, n_lod_own) except the cell's own (sim_kernels.cl:940-955)
     const uint32_t first = L.first_src, last = L.n_lod_own;

@@ -412,8 +412,7 @@ __device__ __forceinline__ void surrogate_tile(const DevLbm& L, const SurSmem& s
         lx = lc % L.bsx; ly = (lc / L.bsx) % L.bsy; lz = lc / (L.bsx * L.bsy);
         return li;
     };
-    Pair3 cp[SC_CPT / 2];  // cell coordinates relative to the bin centre
-    float2 cc[SC_CPT / 2];
+    float rx[SC_CPT], ry[SC_CPT], rz[SC_CPT];  // cell coordinates relative to the bin centre
     FarSums fs[SC_CPT / 2];
     uint32_t live = 0u;  // bit k: cell k exists and is not solid
     const size_t N = L.n;
@@ -431,14 +430,17 @@ __device__ __forceinline__ void surrogate_tile(const DevLbm& L, const SurSmem& s
             asm volatile("prefetch.global.L2 [%0];" ::"l"(L.e_stat + c * N + m));
             asm volatile("prefetch.global.L2 [%0];" ::"l"(L.b_stat + c * N + m));
         }
-        const float fx = (float)x - o.x, fy = (float)y - o.y, fz = (float)z - o.z;
-        lane(cp[k / 2].x, k & 1u) = fx;
-        lane(cp[k / 2].y, k & 1u) = fy;
-        lane(cp[k / 2].z, k & 1u) = fz;
-        lane(cc[k / 2], k & 1u) = fmaf(fz, fz, fmaf(fy, fy, fx * fx));
+        rx[k] = (float)x - o.x; ry[k] = (float)y - o.y; rz[k] = (float)z - o.z;
     }
+    Pair3 cp[SC_CPT / 2];
+    P2 cc[SC_CPT / 2];
 #pragma unroll
-    for (uint32_t j = 0; j < SC_CPT / 2; j++) far_zero(fs[j]);
+    for (uint32_t j = 0; j < SC_CPT / 2; j++) {
+        cp[j] = {pk(rx[2 * j], rx[2 * j + 1]), pk(ry[2 * j], ry[2 * j + 1]), pk(rz[2 * j], rz[2 * j + 1])};
+        cc[j] = pk(fmaf(rz[2 * j], rz[2 * j], fmaf(ry[2 * j], ry[2 * j], rx[2 * j] * rx[2 * j])),
+                   fmaf(rz[2 * j + 1], rz[2 * j + 1], fmaf(ry[2 * j + 1], ry[2 * j + 1], rx[2 * j + 1] * rx[2 * j + 1])));
+        far_zero(fs[j]);
+    }
     const uint32_t cnt = sm.count;
 #pragma unroll 1
     for (uint32_t s = 0; s < cnt; s++) {
