@@ -58,8 +58,10 @@ sys.path.insert(0, str(ROOT))
 FLOP_PER_INTERACTION = 34  # one source's E and B: 34 FLOP + 1 sqrt (sim_kernels.cl:950-954)
 # kernel-time results of one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum per launch);
 # the summaries with the commands that produced them are in profiles/
-NCU_TRAFFIC = {("tgv256", "k_stream_collide"): 2.506905e9, ("mhd128", "k_stream_collide"): 0.797089e9,
-               ("mhd128", "k_update_e_b_fast"): 59.139e6}
+# (rings384: the 192^3 capture of the same kernel scaled by the cell count, 8x; its traffic is
+# proportional to the cells)
+NCU_TRAFFIC = {("tgv256", "k_stream_collide"): 2.507149e9, ("mhd128", "k_stream_collide"): 0.795728e9,
+               ("mhd128", "k_update_e_b_fast"): 63.567e6, ("rings384", "k_stream_collide"): 12.8329e9}
 
 
 def parse():

@@ -238,6 +238,24 @@ int ion_lbm_set_kernel_timing(ion_lbm* h, int enable);
 int ion_lbm_kernel_time(ion_lbm* h, int kernel, double* total_ms, uint64_t* launches);
 int ion_lbm_reset_kernel_time(ion_lbm* h);
 
+/* ---- LbmConfig as JSON (file::read_config / file::write_config,
+ *      src/file.rs:310-334; serde's layout of LbmConfig, src/lbm/mod.rs:45-101).
+ *      Reading maps graphics_config.graphics_active to update_fields and
+ *      ignores the other graphics settings; writing emits GraphicsConfig::new()
+ *      with graphics_active = update_fields, plus a "field_mode" key that the
+ *      reference ignores.  No device is needed. ---------------------------- */
+int ion_config_write_json(const char* path, const ion_config* cfg);
+int ion_config_read_json(const char* path, ion_config* cfg);
+
+/* ---- full checkpoint (no reference counterpart: the reference resumes a
+ *      .ion file from equilibrium, src/file.rs:42-188).  The file is the .ion
+ *      image of ion_lbm_save followed by an extension block ("IONX") with the
+ *      time step and every device buffer the next step reads (DDFs of all
+ *      lattices, E/B, LOD bins, force field), so a restored handle continues
+ *      bit for bit.  ion_lbm_load reads such a file as a plain .ion file. --- */
+int ion_lbm_checkpoint(ion_lbm* h, const char* path);
+int ion_lbm_restore(const char* path, ion_config* cfg, ion_lbm** out);
+
 /* ---- learned far field (no reference counterpart; it stands in for the far
  *      part of update_e_b_dynamic, src/kernels/sim_kernels.cl:940-955).
  *      Per cell, LOD bins within Chebyshev distance 2 of the cell's own bin

@@ -94,6 +94,10 @@ _SIGS = {
     "ion_lbm_reset_kernel_time": (C.c_int, [_P]),
     "ion_codec_roundtrip": (C.c_int, [C.c_int, _P, _P, _P, _P, _P, C.c_uint64]),
     "ion_ddf_sum_f64_noalloc": (C.c_int, [_P, C.c_int, C.c_uint64, _P, _P]),
+    "ion_config_write_json": (C.c_int, [C.c_char_p, C.POINTER(Config)]),
+    "ion_config_read_json": (C.c_int, [C.c_char_p, C.POINTER(Config)]),
+    "ion_lbm_checkpoint": (C.c_int, [_P, C.c_char_p]),
+    "ion_lbm_restore": (C.c_int, [C.c_char_p, C.POINTER(Config), C.POINTER(_P)]),
     "ion_lbm_surrogate_train": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, C.c_uint64,
                                           C.POINTER(C.c_float)]),
     "ion_lbm_surrogate_info": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),

@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
               "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-v", f"-I{REPO / 'include'}", f"-I{CSRC}"]
 SOURCES = ["lbm_q19.cu", "lbm_q15.cu", "lbm_q9.cu", "field_kernels.cu", "setup_kernels.cu", "batch_kernels.cu",
-           "noalloc.cu", "surrogate.cu", "ion_api.cu"]
+           "noalloc.cu", "surrogate.cu", "config_json.cpp", "ion_api.cu"]
 
 
 def nvcc() -> str:

@@ -960,7 +960,10 @@ int ion_lbm_load(const char* path, ion_config* cfg, ion_lbm** out) {
     if (buf.size() - r.pos < body) return fail(ION_E_FORMAT, "Not all data could be read, file may be corrupted.");
     const size_t o = r.pos;
     r.pos += body;
-    if (c.ext_magneto_hydro && r.pos != buf.size()) {
+    const bool ext_block = buf.size() - r.pos >= 4 && memcmp(buf.data() + r.pos, "IONX", 4) == 0;
+    if (ext_block) {
+        r.pos = buf.size();  // a checkpoint's extension block: read as a plain .ion file here
+    } else if (c.ext_magneto_hydro && r.pos != buf.size()) {
         // fixed charges and magnets (FILE_LAYOUT.txt:46-58): read and discarded,
         // as the reference does; the reference's writer omits both sections.
         const uint32_t nc = r.u32();
@@ -978,6 +981,110 @@ int ion_lbm_load(const char* path, ion_config* cfg, ion_lbm** out) {
     if (!rc) rc = ion_lbm_write_field(h, ION_FIELD_U, buf.data() + o + 5 * N, 12 * N);
     if (!rc && c.ext_magneto_hydro) rc = ion_lbm_write_field(h, ION_FIELD_Q, buf.data() + o + 17 * N, 4 * N);
     if (rc) { destroy_handle(h); return rc; }
+    *cfg = c;
+    *out = h;
+    return ION_OK;
+}
+
+// ---- full checkpoint ------------------------------------------------------------
+// Extension block after the .ion image: "IONX", u32 version (1), u64 time step,
+// u8 update_fields, u8 field_mode, u8 propellant, u8 0, f32 units.k, u32 section
+// count, then per section u32 field id, u64 bytes, the raw device contents.
+namespace {
+const int kCheckpointFields[] = {ION_FIELD_FI, ION_FIELD_F, ION_FIELD_E_STAT, ION_FIELD_B_STAT, ION_FIELD_E_DYN,
+                                 ION_FIELD_B_DYN, ION_FIELD_FQI, ION_FIELD_EI, ION_FIELD_QU_LOD};
+}
+
+int ion_lbm_checkpoint(ion_lbm* h, const char* path) {
+    if (!h || !path) return fail(ION_E_INVALID, "null argument");
+    if (!h->initialized) return fail(ION_E_STATE, "checkpoint of a handle that was not initialized");
+    int rc = ion_lbm_save(h, path);
+    if (rc) return rc;
+    std::vector<unsigned char> b;
+    const char* magic = "IONX";
+    b.insert(b.end(), magic, magic + 4);
+    push32(b, 1u);
+    push32(b, (uint32_t)(h->t & 0xFFFFFFFFu));
+    push32(b, (uint32_t)(h->t >> 32));
+    b.push_back(h->cfg.update_fields);
+    b.push_back(h->cfg.field_mode);
+    b.push_back((unsigned char)h->cfg.units.prop);
+    b.push_back(0);
+    pushf(b, h->cfg.units.k);
+    std::vector<std::pair<int, size_t>> secs;
+    for (int id : kCheckpointFields) {
+        size_t eb = 0, cnt = 0;
+        if (ion_lbm_field_info(h, id, &eb, &cnt) == ION_OK && eb * cnt > 0) secs.push_back({id, eb * cnt});
+    }
+    push32(b, (uint32_t)secs.size());
+    for (auto& sc : secs) {
+        push32(b, (uint32_t)sc.first);
+        push32(b, (uint32_t)(sc.second & 0xFFFFFFFFu));
+        push32(b, (uint32_t)((uint64_t)sc.second >> 32));
+        const size_t at = b.size();
+        b.resize(at + sc.second);
+        rc = ion_lbm_read_field(h, sc.first, b.data() + at, sc.second);
+        if (rc) return rc;
+    }
+    std::ofstream f(path, std::ios::binary | std::ios::app);
+    if (!f) return fail(ION_E_IO, "writing went wrong: cannot open \"%s\"", path);
+    f.write((const char*)b.data(), (std::streamsize)b.size());
+    if (!f) return fail(ION_E_IO, "writing went wrong: \"%s\"", path);
+    return ION_OK;
+}
+
+int ion_lbm_restore(const char* path, ion_config* cfg, ion_lbm** out) {
+    if (!path || !cfg || !out) return fail(ION_E_INVALID, "null argument");
+    *out = nullptr;
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return fail(ION_E_IO, "Could not find file.");
+    std::vector<unsigned char> buf((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    // locate the extension block: it follows the .ion body, whose size the header gives
+    if (buf.size() < 16 + 62) return fail(ION_E_FORMAT, "Invalid Format!");
+    Reader hr{buf};
+    hr.pos = 16 + 3 + 16;
+    const uint32_t nx = hr.u32(), ny = hr.u32(), nz = hr.u32();
+    hr.pos = 16 + 62 - 2;
+    const bool mhd = (hr.u8() & 8) != 0;
+    const uint64_t N = (uint64_t)nx * ny * nz;
+    const uint64_t ext_at = 16 + 62 + N * 17 + (mhd ? 4 * N : 0);
+    if (!hr.ok || ext_at + 4 > buf.size() || memcmp(buf.data() + ext_at, "IONX", 4) != 0)
+        return fail(ION_E_FORMAT, "\"%s\" is not a checkpoint (no extension block)", path);
+    Reader r{buf};
+    r.pos = ext_at + 4;
+    const uint32_t version = r.u32();
+    const uint64_t t = (uint64_t)r.u32() | ((uint64_t)r.u32() << 32);
+    const uint8_t update_fields = r.u8(), field_mode = r.u8(), prop = r.u8();
+    r.u8();
+    const float unit_k = r.f32();
+    const uint32_t nsec = r.u32();
+    if (!r.ok || version != 1u) return fail(ION_E_FORMAT, "unsupported checkpoint version");
+    ion_config c = *cfg;
+    c.update_fields = update_fields;
+    c.field_mode = field_mode;
+    c.units.prop = prop;
+    c.units.k = unit_k;
+    ion_lbm* h = nullptr;
+    int rc = ion_lbm_load(path, &c, &h);
+    if (rc) return rc;
+    for (uint32_t k = 0; k < nsec && !rc; k++) {
+        const uint32_t id = r.u32();
+        const uint64_t bytes = (uint64_t)r.u32() | ((uint64_t)r.u32() << 32);
+        if (!r.ok || buf.size() - r.pos < bytes) { rc = fail(ION_E_FORMAT, "checkpoint truncated"); break; }
+        size_t eb = 0, cnt = 0;
+        if (ion_lbm_field_info(h, (int)id, &eb, &cnt) != ION_OK || eb * cnt != bytes) {
+            rc = fail(ION_E_FORMAT, "checkpoint section %u does not match the configuration", id);
+            break;
+        }
+        rc = ion_lbm_write_field(h, (int)id, buf.data() + r.pos, (size_t)bytes);
+        r.pos += bytes;
+    }
+    if (!rc && r.pos != buf.size()) rc = fail(ION_E_FORMAT, "Not all data could be read, file may be corrupted.");
+    if (!rc && cudaStreamSynchronize(h->stream) != cudaSuccess) rc = fail(ION_E_CUDA, "restore");
+    if (rc) { destroy_handle(h); return rc; }
+    h->t = t;
+    h->initialized = true;
+    h->graph_dirty = true;
     *cfg = c;
     *out = h;
     return ION_OK;

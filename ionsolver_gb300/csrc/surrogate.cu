@@ -829,10 +829,12 @@ void Surrogate::infer_bf16(const float* X, cudaStream_t s) {
     auto conv = [&](const __nv_bfloat16* in, int l, const float* res, float* out, __nv_bfloat16* outb) {
         const LayerDef& d = kLayers[l];
         const __nv_bfloat16* wk = wk_ + wkoff_[l];
-        static_assert(OUT_PAD == 21 * 8, "head n-tiles");
-        if (l == 0) k_conv_bf16<16, 4><<<dim3(gx, 1), 128, 0, s>>>(in, wk, res, out, outb, d.cout, d.dil, nd_);
-        else if (d.cout == 32) k_conv_bf16<32, 4><<<dim3(gx, 1), 128, 0, s>>>(in, wk, res, out, outb, d.cout, d.dil, nd_);
-        else k_conv_bf16<32, 7><<<dim3(gx, 3), 128, 0, s>>>(in, wk, res, out, outb, d.cout, d.dil, nd_);
+        static_assert(OUT_PAD == 21 * 8 && 32 == 4 * 8, "n-tiles of 8 channels");
+        // one n-tile (8 channels) per warp: 4x (21x for the head) more warps than voxel tiles,
+        // which these latency-bound launches need to fill the GPU
+        if (l == 0) k_conv_bf16<16, 1><<<dim3(gx, 4), 128, 0, s>>>(in, wk, res, out, outb, d.cout, d.dil, nd_);
+        else if (d.cout == 32) k_conv_bf16<32, 1><<<dim3(gx, 4), 128, 0, s>>>(in, wk, res, out, outb, d.cout, d.dil, nd_);
+        else k_conv_bf16<32, 1><<<dim3(gx, 21), 128, 0, s>>>(in, wk, res, out, outb, d.cout, d.dil, nd_);
     };
     conv(xb_, 0, nullptr, ha_, ab_);  // h0
     for (int i = 0; i < 4; i++) {

@@ -335,6 +335,18 @@ class Lbm:
         N.check(N.lib().ion_lbm_load(str(path).encode(), C.byref(c), C.byref(h)))
         return Lbm(_handle=h)
 
+    def checkpoint(self, path: str) -> None:
+        """Full state (the .ion image + every buffer the next step reads + the time step)."""
+        N.check(N.lib().ion_lbm_checkpoint(self._h, str(path).encode()))
+
+    @staticmethod
+    def restore(path: str, config: LbmConfig | None = None) -> "Lbm":
+        """A handle that continues a checkpoint bit for bit (no initialize() needed)."""
+        c = (config or LbmConfig()).to_c()
+        h = C.c_void_p()
+        N.check(N.lib().ion_lbm_restore(str(path).encode(), C.byref(c), C.byref(h)))
+        return Lbm(_handle=h)
+
     # -- learned far field ----------------------------------------------------------------
     def surrogate_train(self, samples: int = 2000, epochs: int = 20, batch: int = 8, lr: float = 1e-3,
                         seed: int = 5) -> float:
@@ -423,6 +435,18 @@ class Lbm:
 
     def reset_kernel_time(self) -> None:
         N.check(N.lib().ion_lbm_reset_kernel_time(self._h))
+
+
+def write_config(path: str, cfg: LbmConfig) -> None:
+    """LbmConfig as JSON in the reference's serde layout (file::write_config, src/file.rs:324-334)."""
+    N.check(N.lib().ion_config_write_json(str(path).encode(), C.byref(cfg.to_c())))
+
+
+def read_config(path: str) -> LbmConfig:
+    """LbmConfig from the reference's JSON (file::read_config, src/file.rs:310-322)."""
+    c = N.Config()
+    N.check(N.lib().ion_config_read_json(str(path).encode(), C.byref(c)))
+    return LbmConfig.from_c(c)
 
 
 class Batch:
