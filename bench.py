@@ -67,7 +67,7 @@ NCU_TRAFFIC = {("tgv256", "k_stream_collide"): 2.507149e9, ("mhd128", "k_stream_
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=50)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="mhd128",
@@ -198,7 +198,7 @@ class Dist:
 
 
 class Clocks:
-    """nvidia-smi samples every 200 ms; the summary uses the samples taken inside the timed window."""
+    """nvidia-smi samples every 50 ms; the summary uses the samples taken inside the timed window."""
     QUERY = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
@@ -215,7 +215,7 @@ class Clocks:
             self.path.parent.mkdir(exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
             time.sleep(0.5)
         except Exception:

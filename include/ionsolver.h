@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define ION_ABI_VERSION 1
+#define ION_ABI_VERSION 2
 
 /* ---- status codes ---------------------------------------------------- */
 #define ION_OK 0
@@ -72,7 +72,10 @@ enum {
     ION_FIELD_EI = 10,     /* electron-gas DDFs, [q][N], f32 or u16        */
     ION_FIELD_Q = 11,      /* f32 [N] cell charge                          */
     ION_FIELD_QU_LOD = 12, /* f32 [n_lod][4] charge + velocity LOD         */
-    ION_FIELD_COUNT = 13
+    ION_FIELD_E_VAR = 13,  /* f32 [3][N] oscillating field (ext_subgrid_ecr) */
+    ION_FIELD_ETI = 14,    /* electron-temperature DDFs, [7][N], f32 or u16 */
+    ION_FIELD_ET = 15,     /* f32 [N] electron temperature                 */
+    ION_FIELD_COUNT = 16
 };
 
 /* ModelType -> flag byte, src/mesh.rs:9-14, 309-314 */
@@ -100,7 +103,7 @@ typedef struct ion_config {
     uint8_t ext_volume_force;
     uint8_t ext_force_field;
     uint8_t ext_magneto_hydro;
-    uint8_t ext_subgrid_ecr;       /* not supported: must be 0 */
+    uint8_t ext_subgrid_ecr;       /* needs ext_magneto_hydro  */
     uint8_t mhd_lod_depth;
     uint8_t update_fields;
     uint8_t field_mode;            /* ION_FIELD_*              */
@@ -122,6 +125,8 @@ typedef struct ion_constants {
     float wq;       /* DEF_WQ  = 1/(2 k_charge_expansion + 1/2) */
     float epsilon_0;/* epsilon_0_lu                        */
     float mu_0;     /* mu_0_lu                             */
+    float kkbme;    /* DEF_KKBME = kkBme_lu (SUBGRID_ECR)  */
+    float keabs;    /* DEF_KEABS = keabs_lu (SUBGRID_ECR)  */
 } ion_constants;
 
 typedef struct ion_lbm ion_lbm;   /* opaque: Lbm with its single LbmDomain */
@@ -213,6 +218,9 @@ int ion_lbm_voxelise_mesh(ion_lbm* h, uint32_t index, int model_type, float v0, 
 int ion_lbm_precompute_b(ion_lbm* h);
 /* Lbm::precompute_E, src/lbm/mod.rs:302-314 (static E of charged solids) */
 int ion_lbm_precompute_e(ion_lbm* h);
+/* Lbm::precompute_E_ECR (src/lbm/mod.rs:319-331): the field of ChargedECR /
+ * Charged cells into E_var, the oscillating field of the SUBGRID_ECR extension */
+int ion_lbm_precompute_e_ecr(ion_lbm* h);
 
 /* ---- FP64 domain reductions (no reference counterpart) ----------------- */
 /* sum of rho and of Q over non-solid cells, accumulated in double */
@@ -334,6 +342,13 @@ int ion_batch_event_elapsed(ion_batch* b, int start, int end, float* ms);
  * reads, so nothing needs clearing between calls. */
 #define ION_NOALLOC_MAX_VALUES 268435456ull
 int ion_ddf_sum_f64_noalloc(const void* d_values, int float_type, uint64_t count, double* d_sum, void* stream);
+
+/* ---- self-test of the BITWISE field's division (no reference counterpart):
+ *      compares, bit for bit, the quotient formed from one correctly rounded
+ *      reciprocal and two FMA corrections (used for the three divides by
+ *      |R|^3 of sim_kernels.cl:931-935) with the IEEE division on `samples`
+ *      pseudo-random operands in the ranges the E/B sums produce. ------- */
+int ion_check_shared_division(uint64_t samples, uint64_t seed, uint64_t* mismatches, float* first_bad);
 
 /* ---- storage codecs on the device (no reference counterpart; exposes the
  *      FP16S/FP16C codecs of src/lbm/domain.rs:773-780 and

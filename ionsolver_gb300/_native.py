@@ -46,7 +46,7 @@ class Config(C.Structure):
 
 class Constants(C.Structure):
     _fields_ = [(n, C.c_float) for n in ("w", "ke", "kmu", "kmu0", "kkge", "kimg", "kvev", "kme", "wq",
-                                          "epsilon_0", "mu_0")]
+                                          "epsilon_0", "mu_0", "kkbme", "keabs")]
 
 
 # exported symbols and their signatures (every declaration of include/ionsolver.h)
@@ -84,6 +84,7 @@ _SIGS = {
     "ion_lbm_voxelise_mesh": (C.c_int, [_P, C.c_uint32, C.c_int, C.c_float, C.c_float, C.c_float]),
     "ion_lbm_precompute_b": (C.c_int, [_P]),
     "ion_lbm_precompute_e": (C.c_int, [_P]),
+    "ion_lbm_precompute_e_ecr": (C.c_int, [_P]),
     "ion_lbm_mass_charge": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "ion_lbm_save": (C.c_int, [_P, C.c_char_p]),
     "ion_lbm_load": (C.c_int, [C.c_char_p, C.POINTER(Config), C.POINTER(_P)]),
@@ -92,6 +93,7 @@ _SIGS = {
     "ion_lbm_set_kernel_timing": (C.c_int, [_P, C.c_int]),
     "ion_lbm_kernel_time": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
     "ion_lbm_reset_kernel_time": (C.c_int, [_P]),
+    "ion_check_shared_division": (C.c_int, [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_float)]),
     "ion_codec_roundtrip": (C.c_int, [C.c_int, _P, _P, _P, _P, _P, C.c_uint64]),
     "ion_ddf_sum_f64_noalloc": (C.c_int, [_P, C.c_int, C.c_uint64, _P, _P]),
     "ion_config_write_json": (C.c_int, [C.c_char_p, C.POINTER(Config)]),

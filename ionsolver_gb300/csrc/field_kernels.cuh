@@ -179,7 +179,8 @@ __device__ __forceinline__ void add_src(float rx, float ry, float rz, float4 val
         // val = (q, vx, vy, vz); sim_kernels.cl:931-935 / 950-954
         const float s = sqrtf((rx * rx + ry * ry) + rz * rz);
         const float c3 = (s * s) * s;
-        const float px = rx / c3, py = ry / c3, pz = rz / c3;
+        const float y = __frcp_rn(c3);  // the three IEEE divides by c3, via one reciprocal
+        const float px = div_rn_shared(rx, c3, y), py = div_rn_shared(ry, c3, y), pz = div_rn_shared(rz, c3, y);
         e[0] = e[0] + val.x * px; e[1] = e[1] + val.x * py; e[2] = e[2] + val.x * pz;
         const float bx = val.z * pz - val.w * py, by = val.w * px - val.y * pz, bz = val.y * py - val.z * px;
         b[0] = b[0] + val.x * bx; b[1] = b[1] + val.x * by; b[2] = b[2] + val.x * bz;

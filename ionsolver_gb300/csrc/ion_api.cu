@@ -95,6 +95,11 @@ void derive_constants(const ion_config& c, ion_constants& k) {
     k.kvev = (float)(9.1093837139E-31 / (2.0 * 1.602176634E-19) / (double)u.kg);
     k.kme = (float)(5.68563006E-12 / ((double)u.kg / ((double)u.a * (double)u.s)));
     k.wq = 1.0f / (2.0f * 1.0f + 0.5f);
+    // SUBGRID_ECR (units.rs:187-193)
+    k.kkbme = (float)(-22734499.72063751808909449412 /
+                      (((double)u.m * (double)u.m) / (((double)u.s * (double)u.s) * (double)u.k)));
+    k.keabs = (float)(1.40897016100511360652E-8 /
+                      ((((double)u.a * (double)u.a) * ((double)u.s * (double)u.s)) / (double)u.kg));
 }
 
 int velocity_q(int vs) { return vs == ION_D2Q9 ? 9 : vs == ION_D3Q15 ? 15 : vs == ION_D3Q19 ? 19 : 27; }
@@ -111,7 +116,8 @@ int validate(const ion_config& c) {
     const uint64_t n = (uint64_t)c.n_x * c.n_y * c.n_z;
     if (n >= (1ull << 32)) return fail(ION_E_CONFIG, "more than 2^32-1 cells (the reference indexes cells with uint)");
     if (c.velocity_set == ION_D2Q9 && c.n_z != 1) return fail(ION_E_CONFIG, "D2Q9 needs n_z == 1");
-    if (c.ext_subgrid_ecr) return fail(ION_E_CONFIG, "the SUBGRID_ECR extension is not part of this build");
+    if (c.ext_subgrid_ecr && !c.ext_magneto_hydro)
+        return fail(ION_E_CONFIG, "ext_subgrid_ecr needs ext_magneto_hydro (as in the reference, mod.rs:79-80)");
     if (c.ext_magneto_hydro) {
         if (!c.ext_volume_force) return fail(ION_E_CONFIG, "ext_magneto_hydro needs ext_volume_force (as in the reference)");
         if (c.velocity_set == ION_D2Q9)
@@ -223,12 +229,15 @@ void destroy_handle(ion_lbm* h) {
 }
 
 // -------- launches of one step ---------------------------------------------
+// kernel variant: 0 plain, 1 MAGNETO_HYDRO, 2 MAGNETO_HYDRO + SUBGRID_ECR
+int lbm_mode(const ion_config& c) { return c.ext_magneto_hydro ? (c.ext_subgrid_ecr ? 2 : 1) : 0; }
+
 int launch_stream_collide(ion_lbm* h, uint64_t t) {
-    const int ft = h->cfg.float_type;
-    const bool mhd = h->cfg.ext_magneto_hydro, trt = h->cfg.relaxation_time == ION_TRT;
-    if (h->q == 19) q19_stream_collide(h->L, ft, mhd, trt, t, h->stream);
-    else if (h->q == 15) q15_stream_collide(h->L, ft, mhd, trt, t, h->stream);
-    else q9_stream_collide(h->L, ft, mhd, trt, t, h->stream);
+    const int ft = h->cfg.float_type, mode = lbm_mode(h->cfg);
+    const bool trt = h->cfg.relaxation_time == ION_TRT;
+    if (h->q == 19) q19_stream_collide(h->L, ft, mode, trt, t, h->stream);
+    else if (h->q == 15) q15_stream_collide(h->L, ft, mode, trt, t, h->stream);
+    else q9_stream_collide(h->L, ft, mode, trt, t, h->stream);
     g_launches++;
     CKL();
     return ION_OK;
@@ -509,6 +518,11 @@ int ion_lbm_create(const ion_config* cfg, ion_lbm** out) {
         A((void**)&L.qu_lod, (size_t)n_lod_own * 16);
         if (depth > 0) A((void**)&L.lod_cell, 3 * N * 4);
         A((void**)&L.lod_pos, (size_t)n_lod_own * 16);
+        if (cfg->ext_subgrid_ecr) {  // domain.rs:200-211
+            A((void**)&L.e_var, 3 * N * 4);
+            A(&L.eti, 7 * N * db);
+            A((void**)&L.et, N * 4);
+        }
     }
     A((void**)&h->d_err, 4);
     h->nparts = 1024;
@@ -519,6 +533,7 @@ int ion_lbm_create(const ion_config* cfg, ion_lbm** out) {
     k_fill<<<grid_for(N, 256), 256, 0, h->stream>>>(L.rho, N, 1.0f);  // rho starts at 1 (domain.rs:156)
     g_launches++;
     L.w = h->k.w; L.ke = h->k.ke; L.kmu = h->k.kmu; L.kmu0 = h->k.kmu0; L.kkge = h->k.kkge; L.wq = h->k.wq;
+    L.kkbme = h->k.kkbme; L.keabs = h->k.keabs;
     L.fx = cfg->f_x; L.fy = cfg->f_y; L.fz = cfg->f_z;
     L.ext_eq = cfg->ext_equilibrium_boundaries; L.ext_vf = cfg->ext_volume_force; L.ext_ff = cfg->ext_force_field;
     L.ext_mhd = mhd; L.update_fields = cfg->update_fields; L.trt = cfg->relaxation_time == ION_TRT;
@@ -563,12 +578,12 @@ int ion_lbm_get_config(const ion_lbm* h, ion_config* out) {
 
 int ion_lbm_initialize(ion_lbm* h) {
     if (!h) return fail(ION_E_INVALID, "null handle");
-    const int ft = h->cfg.float_type;
+    const int ft = h->cfg.float_type, mode = lbm_mode(h->cfg);
     const bool mhd = h->cfg.ext_magneto_hydro;
     h->t = 1;
-    if (h->q == 19) q19_initialize(h->L, ft, mhd, h->stream);
-    else if (h->q == 15) q15_initialize(h->L, ft, mhd, h->stream);
-    else q9_initialize(h->L, ft, mhd, h->stream);
+    if (h->q == 19) q19_initialize(h->L, ft, mode, h->stream);
+    else if (h->q == 15) q15_initialize(h->L, ft, mode, h->stream);
+    else q9_initialize(h->L, ft, mode, h->stream);
     g_launches++;
     CKL();
     if (mhd) {
@@ -684,6 +699,9 @@ static void* field_ptr(ion_lbm* h, int f, size_t* eb, size_t* count) {
         case ION_FIELD_EI: p = h->L.ei; e = db; c = mhd ? N * h->q : 0; break;
         case ION_FIELD_Q: p = h->L.q; c = mhd ? N : 0; break;
         case ION_FIELD_QU_LOD: p = h->L.qu_lod; c = mhd ? 4 * (size_t)h->L.n_lod_own : 0; break;
+        case ION_FIELD_E_VAR: p = h->L.e_var; c = h->L.e_var ? 3 * N : 0; break;
+        case ION_FIELD_ETI: p = h->L.eti; e = db; c = h->L.eti ? 7 * N : 0; break;
+        case ION_FIELD_ET: p = h->L.et; c = h->L.et ? N : 0; break;
         default: break;
     }
     if (eb) *eb = e;
@@ -867,7 +885,22 @@ int ion_lbm_precompute_e(ion_lbm* h) {
     if (rc) return rc;
     launch_compact(h->L, F_F | F_C, h->d_tiles, h->d_list, h->d_count, h->stream);
     g_launches += 3;
-    launch_static_e(h->L, h->d_list, h->d_count, h->stream);
+    launch_static_e(h->L, h->d_list, h->d_count, h->L.e_stat, h->stream);
+    g_launches++;
+    CKL();
+    CK(cudaStreamSynchronize(h->stream));
+    return ION_OK;
+}
+
+int ion_lbm_precompute_e_ecr(ion_lbm* h) {
+    if (!h) return fail(ION_E_INVALID, "null handle");
+    if (!h->cfg.ext_magneto_hydro || !h->cfg.ext_subgrid_ecr)
+        return fail(ION_E_STATE, "precompute_e_ecr needs ext_magneto_hydro and ext_subgrid_ecr");
+    int rc = ensure_compaction(h);
+    if (rc) return rc;
+    launch_compact(h->L, F_F | F_C, h->d_tiles, h->d_list, h->d_count, h->stream);
+    g_launches += 3;
+    launch_static_e(h->L, h->d_list, h->d_count, h->L.e_var, h->stream);  // domain.rs:569-578
     g_launches++;
     CKL();
     CK(cudaStreamSynchronize(h->stream));
@@ -991,8 +1024,9 @@ int ion_lbm_load(const char* path, ion_config* cfg, ion_lbm** out) {
 // u8 update_fields, u8 field_mode, u8 propellant, u8 0, f32 units.k, u32 section
 // count, then per section u32 field id, u64 bytes, the raw device contents.
 namespace {
-const int kCheckpointFields[] = {ION_FIELD_FI, ION_FIELD_F, ION_FIELD_E_STAT, ION_FIELD_B_STAT, ION_FIELD_E_DYN,
-                                 ION_FIELD_B_DYN, ION_FIELD_FQI, ION_FIELD_EI, ION_FIELD_QU_LOD};
+const int kCheckpointFields[] = {ION_FIELD_FI,  ION_FIELD_F,     ION_FIELD_E_STAT, ION_FIELD_B_STAT,
+                                 ION_FIELD_E_DYN, ION_FIELD_B_DYN, ION_FIELD_FQI,  ION_FIELD_EI,
+                                 ION_FIELD_QU_LOD, ION_FIELD_E_VAR, ION_FIELD_ETI, ION_FIELD_ET};
 }
 
 int ion_lbm_checkpoint(ion_lbm* h, const char* path) {
@@ -1218,6 +1252,7 @@ int ion_batch_create(ion_lbm* const* domains, uint32_t count, ion_batch** out) {
         ion_lbm* h = domains[i];
         if (!h) return fail(ION_E_INVALID, "null domain %u", i);
         if (h->q != 19) return fail(ION_E_CONFIG, "batches run D3Q19 domains");
+        if (h->cfg.ext_subgrid_ecr) return fail(ION_E_CONFIG, "batches do not run the SUBGRID_ECR extension");
         if (h->cfg.float_type != d0->cfg.float_type || h->cfg.ext_magneto_hydro != d0->cfg.ext_magneto_hydro ||
             (h->cfg.ext_magneto_hydro && h->cfg.field_mode != d0->cfg.field_mode))
             return fail(ION_E_CONFIG, "domain %u differs from domain 0 in float type, MHD or field mode", i);
@@ -1586,6 +1621,32 @@ int ion_probe_fp32_peak(double* tflops) {
     if (e != cudaSuccess) return fail(ION_E_CUDA, "fma probe: %s", cudaGetErrorString(e));
     const double flops = 2.0 * 8.0 * (double)iters * 256.0 * (double)blocks;  // FMA = 2 FLOP
     *tflops = flops / (ms * 1e-3) / 1e12;
+    return ION_OK;
+}
+
+int ion_check_shared_division(uint64_t samples, uint64_t seed, uint64_t* mismatches, float* first_bad) {
+    if (!mismatches) return fail(ION_E_INVALID, "null argument");
+    unsigned long long* d_bad = nullptr;
+    float* d_first = nullptr;
+    CK(cudaMalloc(&d_bad, sizeof(unsigned long long)));
+    if (cudaMalloc(&d_first, 2 * sizeof(float)) != cudaSuccess) {
+        cudaFree(d_bad);
+        return fail(ION_E_NOMEM, "division check buffers");
+    }
+    cudaMemset(d_bad, 0, sizeof(unsigned long long));
+    cudaMemset(d_first, 0, 2 * sizeof(float));
+    launch_div_check(samples, seed, d_bad, d_first, 0);
+    g_launches++;
+    unsigned long long bad = 0;
+    float first[2] = {0.0f, 0.0f};
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(&bad, d_bad, sizeof bad, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(first, d_first, sizeof first, cudaMemcpyDeviceToHost);
+    cudaFree(d_bad);
+    cudaFree(d_first);
+    if (e != cudaSuccess) return fail(ION_E_CUDA, "division check: %s", cudaGetErrorString(e));
+    *mismatches = bad;
+    if (first_bad) { first_bad[0] = first[0]; first_bad[1] = first[1]; }
     return ION_OK;
 }
 

@@ -156,6 +156,27 @@ template <> struct Ddf<ION_FP16C> {
     __device__ __forceinline__ static void st(uint16_t* p, size_t i, float x) { p[i] = fp16c_encode(x); }
 };
 
+// x / b rounded to nearest, for finite b > 0, from y = RN(1/b) (__frcp_rn):
+// q0 = RN(x y); the residual r = x - q b is exact under an FMA when q is
+// within a few ulps of x/b; q1 = RN(q0 + r0 y) is within half an ulp plus a
+// tiny term, and Markstein's theorem (P. Markstein, "Computation of
+// elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Dev. 34(1), 1990; also Muller et al., Handbook of Floating-Point
+// Arithmetic, ch. 4) makes q2 = RN(q1 + r1 y) the correctly rounded quotient
+// when y = RN(1/b) and q1 is within one ulp -- barring overflow, underflow and
+// subnormals, which the E/B sums never reach (|x| <= 2^13, 2^-3 <= b <= 2^40,
+// and x = 0 gives +0 as x / b does for x = +0).  Three quotients by the same b
+// then cost one reciprocal and 5 FMA-pipe operations each instead of three
+// full divisions.  ion_check_shared_division compares it bit for bit with the
+// IEEE division on the device.
+__device__ __forceinline__ float div_rn_shared(float x, float b, float y) {
+    float q = x * y;
+    float r = fmaf(-q, b, x);
+    q = fmaf(r, y, q);
+    r = fmaf(-q, b, x);
+    return fmaf(r, y, q);
+}
+
 // ---------------------------------------------------------------------------
 // Device view of one domain (all pointers are device memory).
 // ---------------------------------------------------------------------------
@@ -181,6 +202,10 @@ struct DevLbm {
     uint32_t bsx, bsy, bsz;      // LOD bin extent in cells
     uint32_t near_x, near_y, near_z;  // near-field block extent
     float ils;
+    float* e_var;          // [3][N] SUBGRID_ECR oscillating field (or null)
+    void* eti;             // [7][N] SUBGRID_ECR electron-temperature DDFs (or null)
+    float* et;             // [N]    SUBGRID_ECR electron temperature (or null)
+    float kkbme, keabs;    // DEF_KKBME, DEF_KEABS
     uint8_t ext_eq, ext_vf, ext_ff, ext_mhd, update_fields, trt;
 };
 

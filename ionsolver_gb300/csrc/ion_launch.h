@@ -58,8 +58,8 @@ cudaError_t launch_batch_step(const BatchDev& B, int ft, bool mhd, bool fast, ui
 
 // per velocity set (lbm_q19.cu, lbm_q15.cu, lbm_q9.cu)
 #define ION_DECLARE_LBM_DISPATCH(NAME)                                                                    \
-    void NAME##_stream_collide(const DevLbm& L, int ft, bool mhd, bool trt, uint64_t t, cudaStream_t s);  \
-    void NAME##_initialize(const DevLbm& L, int ft, bool mhd, cudaStream_t s);                            \
+    void NAME##_stream_collide(const DevLbm& L, int ft, int mode, bool trt, uint64_t t, cudaStream_t s);  \
+    void NAME##_initialize(const DevLbm& L, int ft, int mode, cudaStream_t s);                            \
     void NAME##_update_fields(const DevLbm& L, int ft, uint64_t t, cudaStream_t s);
 ION_DECLARE_LBM_DISPATCH(q19)
 ION_DECLARE_LBM_DISPATCH(q15)
@@ -67,11 +67,12 @@ ION_DECLARE_LBM_DISPATCH(q9)
 
 void launch_lod_bins(const DevLbm& L, cudaStream_t s);
 void launch_update_e_b(const DevLbm& L, bool fast, uint32_t* err, cudaStream_t s);
+void launch_div_check(uint64_t samples, uint64_t seed, unsigned long long* bad, float* first_bad, cudaStream_t s);
 void launch_update_e_b_gated(const DevLbm& L, uint32_t* err, const uint32_t* gate, cudaStream_t s);
 void launch_voxelize(const DevLbm& L, const VoxArgs& A, cudaStream_t s);
 void launch_compact(const DevLbm& L, uint8_t mask, uint32_t* tiles, uint32_t* list, uint32_t* total, cudaStream_t s);
 void launch_psi_static_b(const DevLbm& L, const uint32_t* mags, const uint32_t* count, cudaStream_t s);
-void launch_static_e(const DevLbm& L, const uint32_t* list, const uint32_t* count, cudaStream_t s);
+void launch_static_e(const DevLbm& L, const uint32_t* list, const uint32_t* count, float* E, cudaStream_t s);
 void launch_sum_f64(const void* x, int ft, uint64_t count, double* partials, uint32_t nparts, double* out,
                     cudaStream_t s);
 void launch_fma_probe(float* out, int blocks, int iters, cudaStream_t s);

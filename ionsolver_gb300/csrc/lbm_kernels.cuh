@@ -263,7 +263,13 @@ __device__ __forceinline__ void trt_store(typename D::T* f, uint32_t N, uint32_t
 // ---------------------------------------------------------------------------
 // stream_collide, one step (sim_kernels.cl:465-758)
 // ---------------------------------------------------------------------------
-template <int Q, int FT, bool MHD, bool TRT>
+// SUBGRID_ECR (sim_kernels.cl:449-462): |V| at cell m and the gradient of |B_dyn|
+// with the reference's expression a - b / 2 per axis; zero on the domain border
+__device__ __forceinline__ float mag_v(const float* V, size_t N, uint32_t m) {
+    return sqrtf((V[m] * V[m] + V[N + m] * V[N + m]) + V[2 * N + m] * V[2 * N + m]);
+}
+
+template <int Q, int FT, bool MHD, bool TRT, bool ECR = false>
 __device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const bool odd) {
     using V = VSet<Q>;
     using D = Ddf<FT>;
@@ -282,7 +288,7 @@ __device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const
         // MHD: the electron gas first -- it reads no value of the gas lattice, so
         // its DDFs are dead before the gas DDFs are loaded (same values, fewer
         // registers live at once)
-        float rhoe = 0.0f, Bx = 0.0f, By = 0.0f, Bz = 0.0f, Ex = 0.0f, Ey = 0.0f, Ez = 0.0f;
+        float rhoe = 0.0f, Bx = 0.0f, By = 0.0f, Bz = 0.0f, Ex = 0.0f, Ey = 0.0f, Ez = 0.0f, dq_ecr = 0.0f;
         if constexpr (MHD) {
             // the gas and charge lattices are read after the electron gas: start them towards L2
             ep_prefetch<T, Q>((const T*)L.fi, N, n, odd, j);
@@ -294,6 +300,44 @@ __device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const
             ep_load<D, Q>((const T*)L.ei, N, n, odd, j, ehn);
             float uxe, uye, uze;
             moments<V>(ehn, rhoe, uxe, uye, uze);
+            if constexpr (ECR) {  // SUBGRID_ECR, sim_kernels.cl:564-628 (the ionisation term is the reference's placeholder)
+                const Nb7 j7{nb};
+                float ethn[7];
+                ep_load<D, 7>((const T*)L.eti, N, n, odd, j7, ethn);
+                float Etn = 0.0f;
+#pragma unroll
+                for (int i = 0; i < 7; i++) Etn = Etn + ethn[i];
+                Etn = Etn + 1.0f;
+                // ECR heating by the oscillating field's part perpendicular to B
+                const float Evx = L.e_var[n], Evy = L.e_var[(size_t)N + n], Evz = L.e_var[2 * (size_t)N + n];
+                const float lB = sqrtf((Bx * Bx + By * By) + Bz * Bz);
+                const float kpar = ((Evx * Bx + Evy * By) + Evz * Bz) / (lB * lB);
+                const float pex = Evx - kpar * Bx, pey = Evy - kpar * By, pez = Evz - kpar * Bz;
+                const float Emag = sqrtf((pex * pex + pey * pey) + pez * pez);
+                Etn = Etn + (((L.keabs / L.kkbme) * (rhoe + 0.00001f)) / L.kkge) * (Emag * Emag);
+                // guiding-centre drift along -grad |B|
+                float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+                if (!(x == 0u || x == L.nx - 1u || y == 0u || y == L.ny - 1u || z == 0u || z == L.nz - 1u)) {
+                    const uint32_t sx = 1u, sy = L.nx, sz = L.nx * L.ny;
+                    gx = mag_v(L.b_dyn, N, n + sx) - mag_v(L.b_dyn, N, n - sx) / 2.0f;
+                    gy = mag_v(L.b_dyn, N, n + sy) - mag_v(L.b_dyn, N, n - sy) / 2.0f;
+                    gz = mag_v(L.b_dyn, N, n + sz) - mag_v(L.b_dyn, N, n - sz) / 2.0f;
+                }
+                const float kt = L.kkbme * Etn;
+                const float dux = (kt * gx) / lB, duy = (kt * gy) / lB, duz = (kt * gz) / lB;
+                uxe = uxe + dux;
+                uye = uye + duy;
+                uze = uze + duz;
+                Etn = Etn - sqrtf((dux * dux + duy * duy) + duz * duz) / L.kkbme;
+                float eteq[7];
+                adv_equilibrium(Etn, uxe, uye, uze, eteq);
+                if (L.update_fields) L.et[n] = Etn;
+#pragma unroll
+                for (int i = 0; i < 7; i++) ethn[i] = fmaf(1.0f - L.wq, ethn[i], L.wq * eteq[i]);
+                ep_store<D, 7>((T*)L.eti, N, n, odd, j7, ethn);
+                dq_ecr = 0.0001f * Etn;  // ionisation: added to the electron and the gas charge
+                rhoe = rhoe + dq_ecr;
+            }
             const float cxv = uye * Bz - uze * By, cyv = uze * Bx - uxe * Bz, czv = uxe * By - uye * Bx;
             const float nre = -rhoe;
             const float efx = nre * (Ex + cxv), efy = nre * (Ey + cyv), efz = nre * (Ez + czv);
@@ -325,6 +369,7 @@ __device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const
 #pragma unroll
                 for (int i = 0; i < 7; i++) rhoq = rhoq + qhn[i];
                 rhoq = rhoq + 1.0f;
+                if constexpr (ECR) rhoq = rhoq + dq_ecr;
                 float aeq[7];
                 adv_equilibrium(rhoq, uxn, uyn, uzn, aeq);
 #pragma unroll
@@ -365,17 +410,17 @@ __device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const
     }
 }
 
-template <int Q, int FT, bool MHD, bool TRT>
+template <int Q, int FT, bool MHD, bool TRT, bool ECR = false>
 __global__ void __launch_bounds__(256, MHD ? 2 : 4) k_stream_collide(const DevLbm L, const uint32_t odd_t) {
     const bool odd = odd_t != 0u;
     for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < L.n; n += gridDim.x * blockDim.x)
-        sc_cell<Q, FT, MHD, TRT>(L, n, odd);
+        sc_cell<Q, FT, MHD, TRT, ECR>(L, n, odd);
 }
 
 // ---------------------------------------------------------------------------
 // initialize (sim_kernels.cl:760-832): equilibrium DDFs stored with parity 1
 // ---------------------------------------------------------------------------
-template <int Q, int FT, bool MHD>
+template <int Q, int FT, bool MHD, bool ECR = false>
 __global__ void __launch_bounds__(256) k_initialize(const DevLbm L) {
     using V = VSet<Q>;
     using D = Ddf<FT>;
@@ -406,6 +451,10 @@ __global__ void __launch_bounds__(256) k_initialize(const DevLbm L) {
             }
             equilibrium<V>(0.0f, ux, uy, uz, feq);
             ep_store<D, Q>((T*)L.ei, N, n, true, j, feq);
+            if constexpr (ECR) {  // electron temperature DDFs (sim_kernels.cl:827-831)
+                adv_equilibrium(L.et[n], ux, uy, uz, aeq);
+                ep_store<D, 7>((T*)L.eti, N, n, true, j7, aeq);
+            }
         }
     }
 }
@@ -435,35 +484,40 @@ __global__ void __launch_bounds__(256) k_update_fields(const DevLbm L, const uin
     }
 }
 
+// mode: 0 plain, 1 MAGNETO_HYDRO, 2 MAGNETO_HYDRO + SUBGRID_ECR
+template <int QV, int FT>
+void launch_sc(const DevLbm& L, int mode, bool trt, uint32_t o, unsigned g, cudaStream_t s) {
+    if (mode == 2) {
+        if (trt) k_stream_collide<QV, FT, true, true, true><<<g, 256, 0, s>>>(L, o);
+        else k_stream_collide<QV, FT, true, false, true><<<g, 256, 0, s>>>(L, o);
+    } else if (mode == 1) {
+        if (trt) k_stream_collide<QV, FT, true, true><<<g, 256, 0, s>>>(L, o);
+        else k_stream_collide<QV, FT, true, false><<<g, 256, 0, s>>>(L, o);
+    } else {
+        if (trt) k_stream_collide<QV, FT, false, true><<<g, 256, 0, s>>>(L, o);
+        else k_stream_collide<QV, FT, false, false><<<g, 256, 0, s>>>(L, o);
+    }
+}
+template <int QV, int FT>
+void launch_init(const DevLbm& L, int mode, unsigned g, cudaStream_t s) {
+    if (mode == 2) k_initialize<QV, FT, true, true><<<g, 256, 0, s>>>(L);
+    else if (mode == 1) k_initialize<QV, FT, true><<<g, 256, 0, s>>>(L);
+    else k_initialize<QV, FT, false><<<g, 256, 0, s>>>(L);
+}
+
 #define ION_DEFINE_LBM_DISPATCH(QV, NAME)                                                                     \
-    void NAME##_stream_collide(const DevLbm& L, int ft, bool mhd, bool trt, uint64_t t, cudaStream_t s) {      \
+    void NAME##_stream_collide(const DevLbm& L, int ft, int mode, bool trt, uint64_t t, cudaStream_t s) {      \
         const unsigned g = grid_for(L.n, 256);                                                                 \
         const uint32_t o = (uint32_t)(t & 1u);                                                                 \
-        if (ft == ION_FP32) {                                                                                  \
-            if (mhd) { if (trt) k_stream_collide<QV, ION_FP32, true, true><<<g, 256, 0, s>>>(L, o);            \
-                       else k_stream_collide<QV, ION_FP32, true, false><<<g, 256, 0, s>>>(L, o); }             \
-            else { if (trt) k_stream_collide<QV, ION_FP32, false, true><<<g, 256, 0, s>>>(L, o);               \
-                   else k_stream_collide<QV, ION_FP32, false, false><<<g, 256, 0, s>>>(L, o); }                \
-        } else if (ft == ION_FP16S) {                                                                          \
-            if (mhd) { if (trt) k_stream_collide<QV, ION_FP16S, true, true><<<g, 256, 0, s>>>(L, o);           \
-                       else k_stream_collide<QV, ION_FP16S, true, false><<<g, 256, 0, s>>>(L, o); }            \
-            else { if (trt) k_stream_collide<QV, ION_FP16S, false, true><<<g, 256, 0, s>>>(L, o);              \
-                   else k_stream_collide<QV, ION_FP16S, false, false><<<g, 256, 0, s>>>(L, o); }               \
-        } else {                                                                                               \
-            if (mhd) { if (trt) k_stream_collide<QV, ION_FP16C, true, true><<<g, 256, 0, s>>>(L, o);           \
-                       else k_stream_collide<QV, ION_FP16C, true, false><<<g, 256, 0, s>>>(L, o); }            \
-            else { if (trt) k_stream_collide<QV, ION_FP16C, false, true><<<g, 256, 0, s>>>(L, o);              \
-                   else k_stream_collide<QV, ION_FP16C, false, false><<<g, 256, 0, s>>>(L, o); }               \
-        }                                                                                                      \
+        if (ft == ION_FP32) launch_sc<QV, ION_FP32>(L, mode, trt, o, g, s);                                    \
+        else if (ft == ION_FP16S) launch_sc<QV, ION_FP16S>(L, mode, trt, o, g, s);                             \
+        else launch_sc<QV, ION_FP16C>(L, mode, trt, o, g, s);                                                  \
     }                                                                                                          \
-    void NAME##_initialize(const DevLbm& L, int ft, bool mhd, cudaStream_t s) {                                \
+    void NAME##_initialize(const DevLbm& L, int ft, int mode, cudaStream_t s) {                                \
         const unsigned g = grid_for(L.n, 256);                                                                 \
-        if (ft == ION_FP32) { if (mhd) k_initialize<QV, ION_FP32, true><<<g, 256, 0, s>>>(L);                  \
-                              else k_initialize<QV, ION_FP32, false><<<g, 256, 0, s>>>(L); }                   \
-        else if (ft == ION_FP16S) { if (mhd) k_initialize<QV, ION_FP16S, true><<<g, 256, 0, s>>>(L);           \
-                                    else k_initialize<QV, ION_FP16S, false><<<g, 256, 0, s>>>(L); }            \
-        else { if (mhd) k_initialize<QV, ION_FP16C, true><<<g, 256, 0, s>>>(L);                                \
-               else k_initialize<QV, ION_FP16C, false><<<g, 256, 0, s>>>(L); }                                 \
+        if (ft == ION_FP32) launch_init<QV, ION_FP32>(L, mode, g, s);                                          \
+        else if (ft == ION_FP16S) launch_init<QV, ION_FP16S>(L, mode, g, s);                                   \
+        else launch_init<QV, ION_FP16C>(L, mode, g, s);                                                        \
     }                                                                                                          \
     void NAME##_update_fields(const DevLbm& L, int ft, uint64_t t, cudaStream_t s) {                           \
         const unsigned g = grid_for(L.n, 256);                                                                 \

@@ -212,8 +212,9 @@ void launch_psi_static_b(const DevLbm& L, const uint32_t* mags, const uint32_t* 
     k_static_b<<<grid_for(L.n, 256), 256, 0, s>>>(L, L.e_dyn);
 }
 
-// static E from charged solids (charge per cell held in B_dyn.x by the voxeliser)
-__global__ void __launch_bounds__(256) k_static_e(const DevLbm L, const uint32_t* list, const uint32_t* count) {
+// static E from charged solids (charge per cell held in B_dyn.x by the voxeliser) into E:
+// E_stat (static_e_from_mesh) or E_var (precompute_E_ECR, the same kernel)
+__global__ void __launch_bounds__(256) k_static_e(const DevLbm L, const uint32_t* list, const uint32_t* count, float* E) {
     __shared__ float4 s_c[MAG_TILE];
     const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = n < L.n && (L.flags[n] & F_S) != F_S;
@@ -244,14 +245,14 @@ __global__ void __launch_bounds__(256) k_static_e(const DevLbm L, const uint32_t
     }
     if (active) {
         const size_t N = L.n;
-        L.e_stat[n] = L.e_stat[n] + ex * L.ke;
-        L.e_stat[N + n] = L.e_stat[N + n] + ey * L.ke;
-        L.e_stat[2 * N + n] = L.e_stat[2 * N + n] + ez * L.ke;
+        E[n] = E[n] + ex * L.ke;
+        E[N + n] = E[N + n] + ey * L.ke;
+        E[2 * N + n] = E[2 * N + n] + ez * L.ke;
     }
 }
 
-void launch_static_e(const DevLbm& L, const uint32_t* list, const uint32_t* count, cudaStream_t s) {
-    k_static_e<<<grid_for(L.n, 256), 256, 0, s>>>(L, list, count);
+void launch_static_e(const DevLbm& L, const uint32_t* list, const uint32_t* count, float* E, cudaStream_t s) {
+    k_static_e<<<grid_for(L.n, 256), 256, 0, s>>>(L, list, count, E);
 }
 
 // ---------------------------------------------------------------------------
@@ -339,6 +340,52 @@ __global__ void __launch_bounds__(256) k_fma_probe(float* out, int iters, float 
 #pragma unroll
     for (int k = 0; k < 8; k++) s += r[k];
     if (s == 123.456f) out[threadIdx.x] = s;  // keeps the chains alive
+}
+
+// ---------------------------------------------------------------------------
+// Self-test of div_rn_shared against the IEEE division, bit for bit, on
+// pseudo-random quotients over the ranges the E/B sums produce: numerators
+// |x| in [2^-1, 2^13) and exact small integers and halves, denominators
+// b = (s s) s with s = sqrt(r2), r2 in [2^-2, 2^27), and b drawn directly in
+// [2^-3, 2^40).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z += 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ float unit(uint64_t v) { return (float)(v >> 40) * (1.0f / 16777216.0f); }  // [0, 1)
+
+__global__ void __launch_bounds__(256) k_div_check(uint64_t samples, uint64_t seed, unsigned long long* bad,
+                                                   float* first_bad) {
+    unsigned long long local = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < samples;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t h1 = mix64(seed ^ (i * 3 + 0)), h2 = mix64(seed ^ (i * 3 + 1)), h3 = mix64(seed ^ (i * 3 + 2));
+        float x;
+        if ((h1 & 7u) == 0) x = (float)((int)(h1 >> 40) % 16385 - 8192) * 0.5f;  // small integers and halves
+        else x = exp2f(-1.0f + 14.0f * unit(h1)) * ((h1 & 8u) ? -1.0f : 1.0f);
+        float b;
+        if (h2 & 1u) {
+            const float s = sqrtf(exp2f(-2.0f + 29.0f * unit(h2)));
+            b = (s * s) * s;
+        } else {
+            b = exp2f(-3.0f + 43.0f * unit(h2));
+        }
+        b = __uint_as_float(__float_as_uint(b) ^ ((uint32_t)h3 & 0x7u));  // vary the low mantissa bits
+        const float want = __fdiv_rn(x, b);
+        const float got = div_rn_shared(x, b, __frcp_rn(b));
+        if (__float_as_uint(want) != __float_as_uint(got)) {
+            if (atomicAdd(bad, 1ull) == 0ull) { first_bad[0] = x; first_bad[1] = b; }
+            local++;
+        }
+    }
+    (void)local;
+}
+
+void launch_div_check(uint64_t samples, uint64_t seed, unsigned long long* bad, float* first_bad, cudaStream_t s) {
+    k_div_check<<<152 * 8, 256, 0, s>>>(samples, seed, bad, first_bad);
 }
 
 void launch_fma_probe(float* out, int blocks, int iters, cudaStream_t s) {

@@ -43,7 +43,7 @@ class FieldMode(enum.IntEnum):
 
 
 FIELDS = {"fi": 0, "rho": 1, "u": 2, "flags": 3, "F": 4, "e_stat": 5, "b_stat": 6, "e_dyn": 7, "b_dyn": 8,
-          "fqi": 9, "ei": 10, "q": 11, "qu_lod": 12}
+          "fqi": 9, "ei": 10, "q": 11, "qu_lod": 12, "e_var": 13, "eti": 14, "et": 15}
 
 
 @dataclass
@@ -299,6 +299,10 @@ class Lbm:
 
     def precompute_E(self) -> None:
         N.check(N.lib().ion_lbm_precompute_e(self._h))
+
+    def precompute_E_ECR(self) -> None:
+        """Lbm::precompute_E_ECR (src/lbm/mod.rs:319-331): the charges' field into E_var."""
+        N.check(N.lib().ion_lbm_precompute_e_ecr(self._h))
 
     # -- diagnostics ---------------------------------------------------------------
     def mass_charge(self) -> tuple[float, float]:

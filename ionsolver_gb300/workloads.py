@@ -73,6 +73,26 @@ def mhd_box(n: int = 128, float_type: int = 2, depth: int = 4, field_mode: int =
     }
 
 
+def ecr_box(n: int = 32, float_type: int = 2, depth: int = 2, relaxation_time: int = 0, seed_t: int = 9) -> dict:
+    """The SUBGRID_ECR extension on an MHD box: a disk magnet, two ChargedECR plates
+    (+/- 1e-13 C per cell, 1/4 and 3/4 of the box in y) for the oscillating field
+    E_var, an initial electron temperature around 1 (seed 9), 2.45 GHz."""
+    case = mhd_box(n=n, float_type=float_type, depth=depth, magnet_r=n / 4, magnet_t=n / 8)
+    case["config"].update(ext_subgrid_ecr=1, ecr_freq=2.45e9, relaxation_time=relaxation_time)
+    N = n ** 3
+    case["fields"]["et"] = (1.0 + np.random.Generator(np.random.PCG64(seed_t)).normal(0.0, 0.05, N)).astype(np.float32)
+    plates = []
+    for yc, q in ((0.25 * n, 1e-13), (0.75 * n, -1e-13)):
+        p0, p1, p2 = cylinder((0.5 * n, yc, 0.5 * n), n / 5, 2.0, axis=1)
+        case["meshes"].append((p0, p1, p2, "charged_ecr", (q, 0.0, 0.0)))
+        plates.append((p0, p1, p2, "solid", (0.0, 0.0, 0.0)))
+    case["precompute_e_ecr"] = True
+    # after the precomputes the magnet and the plates become solid: the reference's ECR
+    # divides by |B|, which is 0 inside them (static_b_from_mesh skips such cells)
+    case["meshes_after"] = [case["meshes"][0][:3] + ("solid", (0.0, 0.0, 0.0))] + plates
+    return case
+
+
 def batch_domains(count: int = 96, float_type: int = 2, field_mode: int = 1, seed_sizes: int = 3,
                   seed_magnets: int = 4) -> list[dict]:
     """Uneven MHD domains: cube edges uniform from {32,48,64,80,96} (PCG64
@@ -123,3 +143,8 @@ def apply_case(lbm, case: dict) -> None:
         lbm.voxelise_mesh(idx, ModelType(MODEL_IDS[model], tuple(vals)))
     if case["precompute_b"]:
         lbm.precompute_B()
+    if case.get("precompute_e_ecr"):
+        lbm.precompute_E_ECR()
+    for p0, p1, p2, model, vals in case.get("meshes_after", []):
+        idx = lbm.add_mesh(p0, p1, p2)
+        lbm.voxelise_mesh(idx, ModelType(MODEL_IDS[model], tuple(vals)))

@@ -49,11 +49,11 @@ class IonConfig(C.Structure):
 
 class IonConstants(C.Structure):
     _fields_ = [(n, C.c_float) for n in ("w", "ke", "kmu", "kmu0", "kkge", "kimg", "kvev", "kme", "wq",
-                                          "epsilon_0", "mu_0")]
+                                          "epsilon_0", "mu_0", "kkbme", "keabs")]
 
 
 FIELDS = {"fi": 0, "rho": 1, "u": 2, "flags": 3, "F": 4, "e_stat": 5, "b_stat": 6, "e_dyn": 7, "b_dyn": 8,
-          "fqi": 9, "ei": 10, "q": 11, "qu_lod": 12}
+          "fqi": 9, "ei": 10, "q": 11, "qu_lod": 12, "e_var": 13, "eti": 14, "et": 15}
 MODEL = {"solid": 0, "magnet": 1, "charged": 2, "charged_ecr": 3}
 
 
@@ -97,7 +97,8 @@ def _bind(lib: C.CDLL) -> C.CDLL:
     lib.orc_destroy.argtypes = [C.c_void_p]
     lib.orc_field.restype = C.c_void_p
     lib.orc_field.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
-    for f in ("orc_initialize", "orc_do_time_step", "orc_update_fields", "orc_precompute_b", "orc_precompute_e"):
+    for f in ("orc_initialize", "orc_do_time_step", "orc_update_fields", "orc_precompute_b", "orc_precompute_e",
+              "orc_precompute_e_ecr"):
         getattr(lib, f).argtypes = [C.c_void_p]
     lib.orc_run.argtypes = [C.c_void_p, C.c_uint64]
     lib.orc_time_step.restype = C.c_uint64
@@ -260,6 +261,10 @@ class OracleLbm:
     def precompute_e(self):
         self._threads()
         self.lib.orc_precompute_e(self.h)
+
+    def precompute_e_ecr(self):
+        self._threads()
+        self.lib.orc_precompute_e_ecr(self.h)
 
 
 def mesh_bounds(p0, p1, p2):

@@ -111,7 +111,7 @@ def variant_key(cfg: dict) -> str:
     return (f"v{vs}f{ft}r{int(cfg.get('relaxation_time', 0))}e{int(bool(cfg.get('ext_equilibrium_boundaries')))}"
             f"vf{int(bool(cfg.get('ext_volume_force')))}ff{int(bool(cfg.get('ext_force_field')))}"
             f"m{int(bool(cfg.get('ext_magneto_hydro')))}d{int(cfg.get('mhd_lod_depth', 4))}"
-            f"u{int(bool(cfg.get('update_fields')))}")
+            f"u{int(bool(cfg.get('update_fields')))}x{int(bool(cfg.get('ext_subgrid_ecr')))}")
 
 
 def variant_header(cfg: dict) -> str:
@@ -171,6 +171,8 @@ def variant_header(cfg: dict) -> str:
                   "#define DEF_KME ionref::g_kme", f"#define DEF_LOD_DEPTH {d}u",
                   "#define DEF_NUM_LOD ionref::g_num_lod", "#define DEF_NUM_LOD_OWN ionref::g_num_lod_own",
                   "#define DEF_WQ ionref::g_wq"]
+    if cfg.get("ext_subgrid_ecr") and cfg.get("ext_magneto_hydro"):
+        lines += ["#define SUBGRID_ECR", "#define DEF_KKBME ionref::g_kkbme", "#define DEF_KEABS ionref::g_keabs"]
     if cfg.get("ext_force_field"):
         lines.append("#define FORCE_FIELD")
     if cfg.get("update_fields"):

@@ -152,10 +152,11 @@ typedef struct {
     uint64_t t;
     /* constants (get_device_defines, src/lbm/domain.rs:786-858) */
     R w, ke, kmu, kmu0, kkge, wq, wgt[3];
+    R kkbme, keabs; /* SUBGRID_ECR (domain.rs:850-854) */
     /* DDF storage: R (f32/f64) or uint16 (FP16S/FP16C, float build only) */
     int ft; /* storage codec: 0 FP16S, 1 FP16C, 2 native */
-    void *fi, *fqi, *ei;
-    R *rho, *u, *F, *e_stat, *b_stat, *e_dyn, *b_dyn, *qf, *qu_lod;
+    void *fi, *fqi, *ei, *eti;
+    R *rho, *u, *F, *e_stat, *b_stat, *e_dyn, *b_dyn, *qf, *qu_lod, *e_var, *et;
     uint8_t* flags;
     size_t e_dyn_count;
     /* per-cell LOD contributions of the current step */
@@ -216,6 +217,11 @@ int orc_constants(const ion_config* c, ion_constants* k) {
     k->kvev = (float)(9.1093837139E-31 / (2.0 * 1.602176634E-19) / (double)u->kg);
     k->kme = (float)(5.68563006E-12 / ((double)u->kg / ((double)u->a * (double)u->s)));
     k->wq = 1.0f / (2.0f * 1.0f + 0.5f); /* k_charge_expansion_lu() = 1 (units.rs:279-283) */
+    /* SUBGRID_ECR: kkBme_lu, keabs_lu (units.rs:187-193), f64 arithmetic rounded to f32 */
+    k->kkbme = (float)(-22734499.72063751808909449412 /
+                       (((double)u->m * (double)u->m) / (((double)u->s * (double)u->s) * (double)u->k)));
+    k->keabs = (float)(1.40897016100511360652E-8 /
+                       ((((double)u->a * (double)u->a) * ((double)u->s * (double)u->s)) / (double)u->kg));
     return 0;
 }
 
@@ -356,6 +362,52 @@ static uint32_t lod_bin(const orc* h, uint64_t n, uint32_t d) {
 /* ------------------------------------------------------------------------
  * one cell of stream_collide (sim_kernels.cl:465-758)
  * ---------------------------------------------------------------------- */
+/* SUBGRID_ECR block of stream_collide (sim_kernels.cl:557-629) with mag_v /
+ * grad_mag_v (449-461): electron temperature on a D3Q7 lattice, ECR heating
+ * by the part of E_var perpendicular to B, guiding-centre drift along
+ * -grad|B| (the reference's a - b/2 difference), the placeholder ionisation
+ * 1e-4 Et added to the electron and the gas charge. */
+static R mag_v(const orc* h, const R* V, uint64_t m) {
+    const uint64_t N = h->n;
+    return RSQRT((V[m] * V[m] + V[N + m] * V[N + m]) + V[2 * N + m] * V[2 * N + m]);
+}
+static void ecr_cell(orc* h, uint64_t n, const uint64_t* j7, uint64_t t, R Bx, R By, R Bz, R* rhoe, R* rhoq, R* uxe,
+                     R* uye, R* uze) {
+    const uint64_t N = h->n;
+    R ethn[7];
+    ep_load(h, h->eti, 7, n, j7, t, ethn);
+    R Etn = (R)0;
+    for (int i = 0; i < 7; i++) Etn = Etn + ethn[i];
+    Etn = Etn + (R)1;
+    const R Evx = h->e_var[n], Evy = h->e_var[N + n], Evz = h->e_var[2 * N + n];
+    const R lB = RSQRT((Bx * Bx + By * By) + Bz * Bz);
+    const R kpar = ((Evx * Bx + Evy * By) + Evz * Bz) / (lB * lB);
+    const R pex = Evx - kpar * Bx, pey = Evy - kpar * By, pez = Evz - kpar * Bz;
+    const R Emag = RSQRT((pex * pex + pey * pey) + pez * pez);
+    Etn = Etn + (((h->keabs / h->kkbme) * (*rhoe + (R)0.00001f)) / h->kkge) * (Emag * Emag);
+    uint32_t x, y, z;
+    coords(h, n, &x, &y, &z);
+    R gx = (R)0, gy = (R)0, gz = (R)0;
+    if (!(x == 0 || x == h->nx - 1 || y == 0 || y == h->ny - 1 || z == 0 || z == h->nz - 1)) {
+        const uint64_t sy = h->nx, sz = (uint64_t)h->nx * h->ny;
+        gx = mag_v(h, h->b_dyn, n + 1) - mag_v(h, h->b_dyn, n - 1) / (R)2;
+        gy = mag_v(h, h->b_dyn, n + sy) - mag_v(h, h->b_dyn, n - sy) / (R)2;
+        gz = mag_v(h, h->b_dyn, n + sz) - mag_v(h, h->b_dyn, n - sz) / (R)2;
+    }
+    const R kt = h->kkbme * Etn;
+    const R dux = (kt * gx) / lB, duy = (kt * gy) / lB, duz = (kt * gz) / lB;
+    *uxe = *uxe + dux; *uye = *uye + duy; *uze = *uze + duz;
+    Etn = Etn - RSQRT((dux * dux + duy * duy) + duz * duz) / h->kkbme;
+    R eteq[7];
+    adv_equilibrium(Etn, *uxe, *uye, *uze, eteq);
+    if (h->cfg.update_fields) h->et[n] = Etn;
+    for (int i = 0; i < 7; i++) ethn[i] = RFMA((R)1 - h->wq, ethn[i], h->wq * eteq[i]);
+    ep_store(h, h->eti, 7, n, j7, t, ethn);
+    const R dq = (R)0.0001f * Etn;
+    *rhoe = *rhoe + dq;
+    *rhoq = *rhoq + dq;
+}
+
 static void collide_cell(orc* h, uint64_t n, uint64_t t) {
     const vset* vs = h->vs;
     const int q = vs->q;
@@ -396,6 +448,7 @@ static void collide_cell(orc* h, uint64_t n, uint64_t t) {
         R rhoq = (R)0;
         for (int i = 0; i < 7; i++) rhoq = rhoq + qhn[i];
         rhoq = rhoq + (R)1;
+        if (h->eti) ecr_cell(h, n, j7, t, Bx, By, Bz, &rhoe, &rhoq, &uxe, &uye, &uze);
         /* charge advection, part 2 (633-637) */
         h->qf[n] = rhoq - rhoe;
         R aeq[7];
@@ -571,6 +624,7 @@ void* orc_create(const ion_config* cfg, const ion_constants* kin) {
     if (kin) k = *kin; else orc_constants(cfg, &k);
 #ifdef ORC_PREC_F32
     h->w = k.w; h->ke = k.ke; h->kmu = k.kmu; h->kmu0 = k.kmu0; h->kkge = k.kkge; h->wq = k.wq;
+    h->kkbme = k.kkbme; h->keabs = k.keabs;
     if (vs == &VS_D2Q9) { h->wgt[0] = 1.0f / 2.25f; h->wgt[1] = 1.0f / 9.0f; h->wgt[2] = 1.0f / 36.0f; }
     else if (vs == &VS_D3Q15) { h->wgt[0] = 1.0f / 4.5f; h->wgt[1] = 1.0f / 9.0f; h->wgt[2] = 1.0f / 72.0f; }
     else { h->wgt[0] = 1.0f / 3.0f; h->wgt[1] = 1.0f / 18.0f; h->wgt[2] = 1.0f / 36.0f; }
@@ -588,6 +642,8 @@ void* orc_create(const ion_config* cfg, const ion_constants* kin) {
         h->kmu0 = mu0;
         h->kkge = (9.1093837139E-31 / -1.602176634E-19) / ((double)u->kg / ((double)u->a * u->s));
         h->wq = 1.0 / 2.5;
+        h->kkbme = -22734499.72063751808909449412 / (((double)u->m * u->m) / (((double)u->s * u->s) * u->k));
+        h->keabs = 1.40897016100511360652E-8 / ((((double)u->a * u->a) * ((double)u->s * u->s)) / u->kg);
         (void)k;
     }
     if (vs == &VS_D2Q9) { h->wgt[0] = 1.0 / 2.25; h->wgt[1] = 1.0 / 9.0; h->wgt[2] = 1.0 / 36.0; }
@@ -615,6 +671,11 @@ void* orc_create(const ion_config* cfg, const ion_constants* kin) {
         h->qf = (R*)xcalloc(N, sizeof(R));
         h->qu_lod = (R*)xcalloc((size_t)h->n_lod_own * 4, sizeof(R));
         if (h->depth > 0) { h->lodc = (R*)xcalloc(4 * N, sizeof(R)); h->lodm = (uint8_t*)xcalloc(N, 1); }
+        if (cfg->ext_subgrid_ecr) { /* domain.rs:200-211 */
+            h->e_var = (R*)xcalloc(3 * N, sizeof(R));
+            h->eti = xcalloc(7 * N, dsz);
+            h->et = (R*)xcalloc(N, sizeof(R));
+        }
     }
     return h;
 }
@@ -624,7 +685,7 @@ void orc_destroy(void* p) {
     if (!h) return;
     free(h->fi); free(h->fqi); free(h->ei); free(h->rho); free(h->u); free(h->F); free(h->e_stat);
     free(h->b_stat); free(h->e_dyn); free(h->b_dyn); free(h->qf); free(h->qu_lod); free(h->flags);
-    free(h->lodc); free(h->lodm);
+    free(h->lodc); free(h->lodm); free(h->e_var); free(h->eti); free(h->et);
     free(h);
 }
 
@@ -649,6 +710,9 @@ void* orc_field(void* p, int field, size_t* elem_bytes, size_t* count) {
         case ION_FIELD_EI: ptr = h->ei; eb = dsz; c = mhd ? N * h->vs->q : 0; break;
         case ION_FIELD_Q: ptr = h->qf; c = mhd ? N : 0; break;
         case ION_FIELD_QU_LOD: ptr = h->qu_lod; c = mhd ? (size_t)h->n_lod_own * 4 : 0; break;
+        case ION_FIELD_E_VAR: ptr = h->e_var; c = h->e_var ? 3 * N : 0; break;
+        case ION_FIELD_ETI: ptr = h->eti; eb = dsz; c = h->eti ? 7 * N : 0; break;
+        case ION_FIELD_ET: ptr = h->et; c = h->et ? N : 0; break;
         default: break;
     }
     if (elem_bytes) *elem_bytes = eb;
@@ -686,6 +750,10 @@ void orc_initialize(void* p) {
             for (int c = 0; c < 3; c++) { h->b_dyn[c * N + n] = h->b_stat[c * N + n]; h->e_dyn[c * N + n] = h->e_stat[c * N + n]; }
             equilibrium(h, (R)0, h->u[n], h->u[N + n], h->u[2 * N + n], feq);
             ep_store(h, h->ei, q, n, j, 1, feq);
+            if (h->eti) { /* electron temperature DDFs (827-831) */
+                adv_equilibrium(h->et[n], h->u[n], h->u[N + n], h->u[2 * N + n], aeq);
+                ep_store(h, h->eti, 7, n, j7, 1, aeq);
+            }
         }
     }
     if (mhd) field_update(h);
@@ -900,9 +968,19 @@ void orc_precompute_b(void* p) {
 
 /* static_e_from_mesh (sim_kernels.cl:1278-1300): E_stat += k_e sum q r/|r|^3
  * over charged-solid cells (charge held in B_dyn.x by the voxeliser). */
+static void static_e_into(orc* h, R* E);
 void orc_precompute_e(void* p) {
     orc* h = (orc*)p;
     if (!h->cfg.ext_magneto_hydro) return;
+    static_e_into(h, h->e_stat);
+}
+/* Lbm::precompute_E_ECR (mod.rs:319-331): the same kernel into E_var (domain.rs:569-578) */
+void orc_precompute_e_ecr(void* p) {
+    orc* h = (orc*)p;
+    if (!h->e_var) return;
+    static_e_into(h, h->e_var);
+}
+static void static_e_into(orc* h, R* E) {
     const uint64_t N = h->n;
     const long long NN = (long long)N;
 #pragma omp parallel for num_threads(g_threads) schedule(dynamic, 256) if (g_threads > 1)
@@ -922,9 +1000,9 @@ void orc_precompute_e(void* p) {
             const R q = h->b_dyn[i], l3 = (l * l) * l;
             ex = ex + (dx * q) / l3; ey = ey + (dy * q) / l3; ez = ez + (dz * q) / l3;
         }
-        h->e_stat[n] = h->e_stat[n] + ex * h->ke;
-        h->e_stat[N + n] = h->e_stat[N + n] + ey * h->ke;
-        h->e_stat[2 * N + n] = h->e_stat[2 * N + n] + ez * h->ke;
+        E[n] = E[n] + ex * h->ke;
+        E[N + n] = E[N + n] + ey * h->ke;
+        E[2 * N + n] = E[2 * N + n] + ez * h->ke;
     }
 }
 

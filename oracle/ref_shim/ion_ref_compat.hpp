@@ -75,6 +75,8 @@ struct int3 {
 
 inline float3 convert_float3(uint3 v) { return float3((float)v.x, (float)v.y, (float)v.z); }
 
+// OpenCL C's float pi (the value of M_PI_F rounded to float)
+#define M_PI_F 3.14159274101257324219f
 inline float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 inline float3 cross(float3 a, float3 b) {
     return float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);

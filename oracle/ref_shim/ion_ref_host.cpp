@@ -25,7 +25,7 @@ uint g_nx, g_ny, g_nz, g_ax, g_ay, g_az, g_num_lod, g_num_lod_own;
 ulong g_n;
 int g_ox, g_oy, g_oz;
 float g_dox, g_doy, g_doz;
-float g_w, g_ke, g_kmu, g_kmu0, g_kkge, g_kimg, g_kvev, g_kme, g_wq;
+float g_w, g_ke, g_kmu, g_kmu0, g_kkge, g_kimg, g_kvev, g_kme, g_wq, g_kkbme, g_keabs;
 thread_local uint64_t g_gid;
 }  // namespace ionref
 
@@ -77,8 +77,8 @@ struct RefLbm {
     uint q;
     uint n_lod, n_lod_own;
     ulong t;
-    std::vector<fpxx> fi, fqi, ei;
-    std::vector<float> rho, u, F, e_stat, b_stat, e_dyn, b_dyn, qf, qu_lod;
+    std::vector<fpxx> fi, fqi, ei, eti;
+    std::vector<float> rho, u, F, e_stat, b_stat, e_dyn, b_dyn, qf, qu_lod, e_var, et;
     std::vector<uchar> flags;
     std::vector<float> bbu;
 };
@@ -91,6 +91,7 @@ void set_globals(const RefLbm* h) {
     g_num_lod = h->n_lod; g_num_lod_own = h->n_lod_own;
     g_w = h->k.w; g_ke = h->k.ke; g_kmu = h->k.kmu; g_kmu0 = h->k.kmu0; g_kkge = h->k.kkge;
     g_kimg = h->k.kimg; g_kvev = h->k.kvev; g_kme = h->k.kme; g_wq = h->k.wq;
+    g_kkbme = h->k.kkbme; g_keabs = h->k.keabs;
 }
 
 // Units::magnetization_si_lu / charge_si_lu, src/lbm/units.rs:240-257
@@ -142,6 +143,12 @@ void* orc_create(const ion_config* cfg, const ion_constants* k) {
     h->qf.assign(n, 0.0f);
     h->qu_lod.assign((size_t)h->n_lod * 4, 0.0f);
 #endif
+#ifdef SUBGRID_ECR
+    // domain.rs:200-211
+    h->e_var.assign(3 * n, 0.0f);
+    h->eti.assign(7 * n, (fpxx)0);
+    h->et.assign(n, 0.0f);
+#endif
     return h;
 }
 
@@ -165,6 +172,9 @@ void* orc_field(void* p, int field, size_t* elem_bytes, size_t* count) {
         case ION_FIELD_EI: ptr = h->ei.data(); eb = sizeof(fpxx); cnt = h->ei.size(); break;
         case ION_FIELD_Q: ptr = h->qf.data(); cnt = h->qf.size(); break;
         case ION_FIELD_QU_LOD: ptr = h->qu_lod.data(); cnt = h->qu_lod.size(); break;
+        case ION_FIELD_E_VAR: ptr = h->e_var.data(); cnt = h->e_var.size(); break;
+        case ION_FIELD_ETI: ptr = h->eti.data(); eb = sizeof(fpxx); cnt = h->eti.size(); break;
+        case ION_FIELD_ET: ptr = h->et.data(); cnt = h->et.size(); break;
         default: break;
     }
     if (elem_bytes) *elem_bytes = eb;
@@ -196,6 +206,9 @@ void orc_initialize(void* p) {
                    , h->e_stat.data(), h->b_stat.data(), h->e_dyn.data(), h->b_dyn.data(),
                    h->fqi.data(), h->ei.data(), h->qf.data()
 #endif
+#ifdef SUBGRID_ECR
+                   , h->eti.data(), h->et.data()
+#endif
         );
     });
 #ifdef MAGNETO_HYDRO
@@ -221,6 +234,9 @@ void orc_do_time_step(void* p) {
 #ifdef MAGNETO_HYDRO
                        , h->e_dyn.data(), h->b_dyn.data(), h->fqi.data(), h->ei.data(), h->qf.data(),
                        h->qu_lod.data()
+#endif
+#ifdef SUBGRID_ECR
+                       , h->e_var.data(), h->eti.data(), h->et.data(), h->cfg.ecr_freq
 #endif
         );
     });
@@ -308,6 +324,17 @@ void orc_precompute_e(void* p) {
     RefLbm* h = (RefLbm*)p;
     set_globals(h);
     launch(h->n, [&] { static_e_from_mesh(h->flags.data(), h->e_stat.data(), h->b_dyn.data()); });
+#else
+    (void)p;
+#endif
+}
+
+// LbmDomain::enqueue_precompute_e_ecr, src/lbm/domain.rs:569-578
+void orc_precompute_e_ecr(void* p) {
+#ifdef SUBGRID_ECR
+    RefLbm* h = (RefLbm*)p;
+    set_globals(h);
+    launch(h->n, [&] { static_e_from_mesh(h->flags.data(), h->e_var.data(), h->b_dyn.data()); });
 #else
     (void)p;
 #endif

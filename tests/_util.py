@@ -23,6 +23,10 @@ def setup_oracle(case, kind="f32", threads=None, canonical_nan=False):
         o.voxelise(p0, p1, p2, model, vals)
     if case["precompute_b"]:
         o.precompute_b()
+    if case.get("precompute_e_ecr"):
+        o.precompute_e_ecr()
+    for p0, p1, p2, model, vals in case.get("meshes_after", []):
+        o.voxelise(p0, p1, p2, model, vals)
     return o
 
 
@@ -56,6 +60,8 @@ def field_names(case):
     names = ["fi", "rho", "u", "flags"]
     if case["config"].get("ext_magneto_hydro"):
         names += ["fqi", "ei", "q", "e_dyn", "b_dyn", "b_stat", "e_stat", "qu_lod"]
+    if case["config"].get("ext_subgrid_ecr"):
+        names += ["e_var", "eti", "et"]
     return names
 
 
@@ -95,7 +101,7 @@ def compare_bitwise(gpu, orc, names):
         o = orc.field(n)
         if o.dtype != g.dtype:
             o = o.astype(g.dtype)
-        out[n] = bit_diff_nan(g, o, ft if n in ("fi", "fqi", "ei") else None)
+        out[n] = bit_diff_nan(g, o, ft if n in ("fi", "fqi", "ei", "eti") else None)
     return out
 
 

@@ -44,6 +44,10 @@ def geometry():
     return case
 
 
+def ecr(ft, rt):
+    return W.ecr_box(n=16, float_type=ft, depth=2, relaxation_time=rt)
+
+
 CASES = {
     "tgv_fp32_srt": (lambda: plain(2, 0), 20, "run"),
     "tgv_fp16s_trt": (lambda: plain(0, 1), 20, "run"),
@@ -55,4 +59,6 @@ CASES = {
     "mhd16_fp16s_d2": (lambda: mhd(0, 16, 2), 6, "run"),
     "mhd16_fp32_d4": (lambda: mhd(2, 16, 4), 4, "run"),
     "geometry": (geometry, 0, "setup"),
+    "ecr16_fp32_srt": (lambda: ecr(2, 0), 4, "run"),
+    "ecr16_fp16s_trt": (lambda: ecr(0, 1), 3, "run"),
 }

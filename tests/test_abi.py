@@ -29,7 +29,7 @@ def test_library_exports_every_declared_function():
 
 
 def test_abi_version_and_defaults():
-    assert N.lib().ion_abi_version() == 1
+    assert N.lib().ion_abi_version() == 2
     c = N.Config()
     N.check(N.lib().ion_config_default(C.byref(c)))
     # LbmConfig::new (src/lbm/mod.rs:105-135)

@@ -175,3 +175,39 @@ def test_codecs_exhaustive_against_oracle():
         assert np.array_equal(enc, e_ref)
         finite = np.isfinite(d_ref)
         assert np.array_equal(rdec[finite].view(np.uint32), d_ref[finite].view(np.uint32))
+
+
+def test_shared_division_matches_ieee():
+    """The BITWISE field divides by |R|^3 through one correctly rounded reciprocal
+    and two FMA corrections (Markstein); bit for bit the IEEE quotient on 2^30
+    pseudo-random operands in the field's ranges, two seeds."""
+    import ctypes as C
+    from ionsolver_gb300 import _native as N
+    for seed in (1, 0x5eed):
+        bad = C.c_uint64()
+        first = (C.c_float * 2)()
+        N.check(N.lib().ion_check_shared_division(1 << 30, seed, C.byref(bad), first))
+        assert bad.value == 0, (bad.value, first[0], first[1])
+
+
+@pytest.mark.parametrize("ft,rt", [(2, 0), (0, 1), (1, 0)], ids=["FP32-SRT", "FP16S-TRT", "FP16C-SRT"])
+def test_subgrid_ecr_bitwise(ft, rt):
+    """SUBGRID_ECR on the GPU against the oracle: every field bit-identical (NaN =
+    NaN) after two and after four steps; with FP32 storage the first two steps
+    stay finite (16-bit storage reaches the reference's electron-gas NaN sooner)."""
+    case = W.ecr_box(n=16, float_type=ft, depth=2, relaxation_time=rt)
+    names = U.field_names(case)
+    g = U.setup_gpu(case)
+    g.initialize()
+    g.run(2)
+    g.finish_queues(60000)
+    o = orc_run(case, 2)
+    if ft == 2:
+        for n in names:
+            a = g.read(n)
+            assert a.dtype != np.float32 or not np.isnan(a).any(), n
+    assert U.compare_bitwise(g, o, names) == {n: 0 for n in names}
+    g.run(2)
+    g.finish_queues(60000)
+    o.run(2)
+    assert U.compare_bitwise(g, o, names) == {n: 0 for n in names}

@@ -77,6 +77,15 @@ def test_mhd_trt():
     assert_same(a, b, U.field_names(case))
 
 
+@pytest.mark.parametrize("ft,rt", [(2, 0), (0, 1), (1, 0)], ids=["FP32-SRT", "FP16S-TRT", "FP16C-SRT"])
+def test_subgrid_ecr(ft, rt):
+    """SUBGRID_ECR (sim_kernels.cl:449-462, 557-629, 827-831; precompute_E_ECR):
+    electron temperature lattice, ECR heating, drift, ionisation placeholder."""
+    case = W.ecr_box(n=16, float_type=ft, depth=2, relaxation_time=rt)
+    a, b = run_both(case, 4, threads=4)
+    assert_same(a, b, U.field_names(case))
+
+
 def test_voxeliser_and_static_fields():
     case = W.mhd_box(n=16, depth=2, magnet_r=5.0, magnet_t=4.0)
     ring = W.annulus((8.0, 8.0, 11.0), 6.0, 3.0, 2.5, axis=0)
