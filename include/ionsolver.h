@@ -350,6 +350,13 @@ int ion_ddf_sum_f64_noalloc(const void* d_values, int float_type, uint64_t count
  *      pseudo-random operands in the ranges the E/B sums produce. ------- */
 int ion_check_shared_division(uint64_t samples, uint64_t seed, uint64_t* mismatches, float* first_bad);
 
+/* ---- self-test of the learned far field's tcgen05 convolution (no
+ *      reference counterpart): the 3^3 convolution on pseudo-random BF16 data
+ *      through tcgen05.mma (TMEM accumulator) against the mma.sync
+ *      implementation; max |diff| / max |mma.sync result|.  nd^3 must be a
+ *      multiple of 128; (cin, cout) in {(16, 32), (32, 32), (32, 168)}. ---- */
+int ion_check_tcgen05_conv(int nd, int cin, int cout, int dil, uint64_t seed, float* max_rel_err);
+
 /* ---- storage codecs on the device (no reference counterpart; exposes the
  *      FP16S/FP16C codecs of src/lbm/domain.rs:773-780 and
  *      src/kernels/sim_kernels.cl:79-90 for exhaustive checks) ------------ */

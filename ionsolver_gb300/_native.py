@@ -94,6 +94,7 @@ _SIGS = {
     "ion_lbm_kernel_time": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
     "ion_lbm_reset_kernel_time": (C.c_int, [_P]),
     "ion_check_shared_division": (C.c_int, [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_float)]),
+    "ion_check_tcgen05_conv": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(C.c_float)]),
     "ion_codec_roundtrip": (C.c_int, [C.c_int, _P, _P, _P, _P, _P, C.c_uint64]),
     "ion_ddf_sum_f64_noalloc": (C.c_int, [_P, C.c_int, C.c_uint64, _P, _P]),
     "ion_config_write_json": (C.c_int, [C.c_char_p, C.POINTER(Config)]),

@@ -1650,6 +1650,13 @@ int ion_check_shared_division(uint64_t samples, uint64_t seed, uint64_t* mismatc
     return ION_OK;
 }
 
+int ion_check_tcgen05_conv(int nd, int cin, int cout, int dil, uint64_t seed, float* max_rel_err) {
+    if (!max_rel_err) return fail(ION_E_INVALID, "null argument");
+    const int rc = ion::conv_tc_selftest(nd, cin, cout, dil, seed, max_rel_err, 0);
+    g_launches += 4;
+    return rc ? fail(rc, "tcgen05 convolution self-test (nd %d, cin %d, cout %d)", nd, cin, cout) : ION_OK;
+}
+
 // ---- device codec check -------------------------------------------------------
 int ion_codec_roundtrip(int float_type, const float* in, uint16_t* enc, float* dec, const uint16_t* raw, float* raw_dec,
                         uint64_t n) {

@@ -292,12 +292,180 @@ __global__ void __launch_bounds__(128) k_conv_bf16(const __nv_bfloat16* act, con
     }
 }
 
+// ---------------------------------------------------------------------------
+// The same convolution on the 5th-generation tensor cores (tcgen05): one CTA
+// of 4 warps per 128 voxels (M = 128), N = output channels padded to a
+// multiple of 16 (32 or 176), K walked one tap (CIN channels) at a time.  Per
+// tap the CTA gathers the 128 x CIN activation tile and the N x CIN weight
+// tile into shared memory in the canonical K-major layout without swizzle
+// (8-row x 16-byte core matrices; LBO = 128 B between core matrices along K,
+// SBO = CIN/8 x 128 B between 8-row groups), one elected thread issues
+// tcgen05.mma.kind::f16 (BF16 x BF16 -> FP32) into a TMEM accumulator of
+// 128 lanes x N columns and commits to the tile buffer's mbarrier; the two
+// tile buffers alternate, so the gather of tap t+1 overlaps the MMAs of tap
+// t.  The epilogue reads the accumulator with tcgen05.ld (warp w owns TMEM
+// lanes 32w..32w+31 = voxels), adds the residual and writes FP32 and BF16.
+// Waits are bounded; a timeout sets *err and the CTA still frees its TMEM.
+// ---------------------------------------------------------------------------
+namespace tc {
+__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+// shared-memory matrix descriptor: start >> 4 [0,14), LBO >> 4 [16,30), SBO >> 4 [32,46),
+// version 1 [46,48), base offset 0, layout SWIZZLE_NONE (0) [61,64)
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// instruction descriptor, kind::f16: D F32 [4,6) = 1, A BF16 [7,10) = 1, B BF16 [10,13) = 1,
+// A and B K-major (bits 15, 16 = 0), N >> 3 [17,23), M >> 4 [24,29)
+__host__ __device__ constexpr uint32_t idesc_bf16(uint32_t m, uint32_t n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+__device__ __forceinline__ bool wait(uint64_t* bar, uint32_t parity) {
+    for (uint32_t i = 0; i < (1u << 24); i++) {
+        uint32_t done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done) : "r"(saddr(bar)), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+}  // namespace tc
+
+template <int CIN, int NP>
+__global__ void __launch_bounds__(128, 1) k_conv_tc(const __nv_bfloat16* act, const __nv_bfloat16* wkT, const float* res,
+                                                   float* out, __nv_bfloat16* outb, int Cout, int dil, int nd,
+                                                   uint32_t* err) {
+    static_assert(CIN % 16 == 0 && NP % 16 == 0 && NP >= 16 && NP <= 256, "tcgen05 shape");
+    constexpr int K = 27 * CIN;
+    constexpr uint32_t KCOL = CIN / 8;             // core-matrix columns per tap
+    constexpr uint32_t SBO = KCOL * 128u;          // bytes between 8-row groups
+    constexpr uint32_t A_BYTES = 128u * CIN * 2u, B_BYTES = (uint32_t)NP * CIN * 2u;
+    constexpr uint32_t TCOLS = NP <= 32 ? 32 : NP <= 64 ? 64 : NP <= 128 ? 128 : 256;
+    constexpr uint32_t IDESC = tc::idesc_bf16(128, NP);
+    __shared__ __align__(128) uint8_t sa[2][A_BYTES];
+    __shared__ __align__(128) uint8_t sb[2][B_BYTES];
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ uint32_t tmem_slot;
+    const int V = nd * nd * nd;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc::saddr(&bar[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc::saddr(&bar[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc::saddr(&tmem_slot)),
+                     "r"(TCOLS) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+
+    const int v = blockIdx.x * 128 + (int)tid;  // this thread's voxel (A row)
+    const int x = v % nd, y = (v / nd) % nd, z = v / (nd * nd);
+    uint32_t uses[2] = {0u, 0u};
+    bool ok = true;
+    for (int tap = 0; tap < 27 && ok; tap++) {
+        const int buf = tap & 1;
+        if (tap >= 2) {  // the MMAs of tap - 2 read this buffer
+            ok = tc::wait(&bar[buf], (uses[buf] - 1u) & 1u);
+            if (!__syncthreads_and(ok)) break;
+        }
+        // A: this voxel's neighbour at the tap, CIN channels = KCOL x 16 bytes
+        {
+            const int xx = x + dil * tap_off(tap, 0), yy = y + dil * tap_off(tap, 1), zz = z + dil * tap_off(tap, 2);
+            const bool in = v < V && xx >= 0 && yy >= 0 && zz >= 0 && xx < nd && yy < nd && zz < nd;
+            const uint4* src = (const uint4*)(act + (size_t)(in ? xx + (yy + zz * nd) * nd : 0) * CIN);
+            uint8_t* dst = sa[buf] + (tid >> 3) * SBO + (tid & 7u) * 16u;
+#pragma unroll
+            for (uint32_t c = 0; c < KCOL; c++)
+                *(uint4*)(dst + c * 128u) = in ? src[c] : make_uint4(0u, 0u, 0u, 0u);
+        }
+        // B: rows n < Cout of the tap's CIN weights; padded rows are zero
+        for (uint32_t i = tid; i < (uint32_t)NP * KCOL; i += 128u) {
+            const uint32_t n = i / KCOL, c = i % KCOL;
+            const uint4 w = (int)n < Cout ? *(const uint4*)(wkT + (size_t)n * K + tap * CIN + c * 8u)
+                                          : make_uint4(0u, 0u, 0u, 0u);
+            *(uint4*)(sb[buf] + (n >> 3) * SBO + c * 128u + (n & 7u) * 16u) = w;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic stores -> tensor-core reads
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (uint32_t kk = 0; kk < KCOL / 2; kk++) {  // K = 16 per MMA = two core-matrix columns
+                const uint64_t ad = tc::sdesc(tc::saddr(sa[buf]) + kk * 256u, 128u, SBO);
+                const uint64_t bd = tc::sdesc(tc::saddr(sb[buf]) + kk * 256u, 128u, SBO);
+                const uint32_t acc = (tap > 0 || kk > 0) ? 1u : 0u;
+                asm volatile("{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                             " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                             ::"r"(tmem), "l"(ad), "l"(bd), "r"(IDESC), "r"(acc) : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                         ::"r"(tc::saddr(&bar[buf])) : "memory");
+        }
+        uses[buf]++;
+    }
+    // all MMAs done: the last commit of each buffer
+    for (int b = 0; b < 2; b++)
+        if (uses[b] && !tc::wait(&bar[b], (uses[b] - 1u) & 1u)) ok = false;
+    ok = __syncthreads_and(ok) != 0;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok) {
+        const uint32_t row = tmem + ((warp * 32u) << 16);  // this warp's TMEM lanes
+        const int vv = blockIdx.x * 128 + (int)(warp * 32u + lane);
+#pragma unroll 1
+        for (int c0 = 0; c0 < NP; c0 += 8) {
+            uint32_t r[8];
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                           "=r"(r[7])
+                         : "r"(row + (uint32_t)c0));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (vv < V) {
+#pragma unroll
+                for (int e = 0; e < 8; e++) {
+                    const int n = c0 + e;
+                    if (n >= Cout) break;
+                    const size_t o = (size_t)n * V + vv;
+                    const float val = __uint_as_float(r[e]) + (res ? res[o] : 0.0f);
+                    out[o] = val;
+                    if (outb) outb[(size_t)vv * Cout + n] = __float2bfloat16(val);
+                }
+            }
+        }
+    } else if (tid == 0) {
+        atomicExch(err, 1u);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TCOLS) : "memory");
+}
+
 // network input in the inference layout: act [V][16] bf16, channels 4..15 zero
 __global__ void k_input_bf16(const float* X, __nv_bfloat16* act, int V) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V * 16) return;
     const int v = i / 16, c = i % 16;
     act[i] = __float2bfloat16(c < 4 ? X[(size_t)c * V + v] : 0.0f);
+}
+
+// ---------------------------------------------------------------------------
+// self-test: the tcgen05 convolution against the mma.sync one on pseudo-random
+// BF16 activations and weights (same products, FP32 accumulation in another
+// order), max |diff| / max |reference| over FP32 outputs
+// ---------------------------------------------------------------------------
+__global__ void k_fill_bf16(__nv_bfloat16* p, size_t n, uint64_t seed) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint64_t z = seed + i * 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    z ^= z >> 31;
+    p[i] = __float2bfloat16((float)(z >> 40) * (1.0f / 8388608.0f) - 1.0f);
 }
 
 // wkT[co][tap * cinp + ci] = w[co][ci][tap] (zero for the padding channels ci >= cin)
@@ -347,8 +515,15 @@ struct SurSmem {
     float node[Surrogate::OUT_CH];
     // node values contracted along x: t1[lx][iy + 3 iz][c] = sum_ix wx_ix(lx) node[ix + 3 (iy + 3 iz)][c]
     float4 t1[Surrogate::MAX_BLOCK][9][2];
+    // E_stat, B_stat of the tile's cells, fetched with cp.async while the near sums run
+    float stat[6][SC_CELLS];
     uint32_t count;
 };
+
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
 
 __device__ __forceinline__ void quad_weights(float t, float* w) {  // Lagrange weights of the nodes 0, 1/2, 1
     w[0] = 2.0f * (t - 0.5f) * (t - 1.0f);
@@ -356,7 +531,7 @@ __device__ __forceinline__ void quad_weights(float t, float* w) {  // Lagrange w
     w[2] = 2.0f * t * (t - 0.5f);
 }
 
-__device__ __forceinline__ void surrogate_tile(const DevLbm& L, const SurSmem& sm, uint32_t bin, int bx, int by, int bz,
+__device__ __forceinline__ void surrogate_tile(const DevLbm& L, SurSmem& sm, uint32_t bin, int bx, int by, int bz,
                                                uint32_t tile, uint32_t cells, float sE, float sB);
 
 __global__ void __launch_bounds__(SC_THREADS) k_surrogate_cells(const DevLbm L, const float* Y, const float* scales,
@@ -403,7 +578,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_surrogate_cells(const DevLbm L, 
         surrogate_tile(L, sm, bin, bx, by, bz, tile, cells, sE, sB);
 }
 
-__device__ __forceinline__ void surrogate_tile(const DevLbm& L, const SurSmem& sm, uint32_t bin, int bx, int by, int bz,
+__device__ __forceinline__ void surrogate_tile(const DevLbm& L, SurSmem& sm, uint32_t bin, int bx, int by, int bz,
                                                uint32_t tile, uint32_t cells, float sE, float sB) {
     // cell k of this thread: local index li -> (lx, ly, lz) in the bin -> global (x, y, z)
     auto cell = [&](uint32_t k, uint32_t& lx, uint32_t& ly, uint32_t& lz) -> uint32_t {
@@ -423,12 +598,16 @@ __device__ __forceinline__ void surrogate_tile(const DevLbm& L, const SurSmem& s
         const uint32_t li = cell(k, lx, ly, lz);
         const uint32_t x = bx * L.bsx + lx, y = by * L.bsy + ly, z = bz * L.bsz + lz;
         const uint32_t m = x + (y + z * L.ny) * L.nx;
-        if (li < cells && (L.flags[m] & F_BO) != F_S) live |= 1u << k;
-        // the static fields are read after the near sums: start them towards L2 now
+        if (li < cells && (L.flags[m] & F_BO) != F_S) {
+            live |= 1u << k;
+            // the static fields are needed after the near sums: copy them into this
+            // thread's shared-memory slots now (only this thread reads them)
+            const uint32_t slot = k * SC_THREADS + threadIdx.x;
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(L.e_stat + c * N + m));
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(L.b_stat + c * N + m));
+            for (int c = 0; c < 3; c++) {
+                cp_async4(&sm.stat[c][slot], L.e_stat + c * N + m);
+                cp_async4(&sm.stat[3 + c][slot], L.b_stat + c * N + m);
+            }
         }
         rx[k] = (float)x - o.x; ry[k] = (float)y - o.y; rz[k] = (float)z - o.z;
     }
@@ -448,11 +627,13 @@ __device__ __forceinline__ void surrogate_tile(const DevLbm& L, const SurSmem& s
 #pragma unroll
         for (uint32_t j = 0; j < SC_CPT / 2; j++) far_fast2(cp[j], cc[j], S, fs[j]);
     }
+    asm volatile("cp.async.commit_group;\n cp.async.wait_group 0;" ::: "memory");
 #pragma unroll
     for (uint32_t k = 0; k < SC_CPT; k++) {
         if (!(live & (1u << k))) continue;
         uint32_t lx, ly, lz;
         cell(k, lx, ly, lz);
+        const uint32_t slot = k * SC_THREADS + threadIdx.x;
         const uint32_t m = (bx * L.bsx + lx) + ((by * L.bsy + ly) + (bz * L.bsz + lz) * L.ny) * L.nx;
         float e[3] = {0.0f, 0.0f, 0.0f}, b[3] = {0.0f, 0.0f, 0.0f};
         far_finish(cp[k / 2], fs[k / 2], (k & 1u) != 0, e, b);
@@ -468,12 +649,12 @@ __device__ __forceinline__ void surrogate_tile(const DevLbm& L, const SurSmem& s
             far[0] = fmaf(wgt, a.x, far[0]); far[1] = fmaf(wgt, a.y, far[1]); far[2] = fmaf(wgt, a.z, far[2]);
             far[3] = fmaf(wgt, a.w, far[3]); far[4] = fmaf(wgt, b2.x, far[4]); far[5] = fmaf(wgt, b2.y, far[5]);
         }
-        L.e_dyn[m] = L.e_stat[m] + L.ke * (e[0] + sE * far[0]);
-        L.e_dyn[N + m] = L.e_stat[N + m] + L.ke * (e[1] + sE * far[1]);
-        L.e_dyn[2 * N + m] = L.e_stat[2 * N + m] + L.ke * (e[2] + sE * far[2]);
-        L.b_dyn[m] = L.b_stat[m] + L.kmu * (b[0] + sB * far[3]);
-        L.b_dyn[N + m] = L.b_stat[N + m] + L.kmu * (b[1] + sB * far[4]);
-        L.b_dyn[2 * N + m] = L.b_stat[2 * N + m] + L.kmu * (b[2] + sB * far[5]);
+        L.e_dyn[m] = sm.stat[0][slot] + L.ke * (e[0] + sE * far[0]);
+        L.e_dyn[N + m] = sm.stat[1][slot] + L.ke * (e[1] + sE * far[1]);
+        L.e_dyn[2 * N + m] = sm.stat[2][slot] + L.ke * (e[2] + sE * far[2]);
+        L.b_dyn[m] = sm.stat[3][slot] + L.kmu * (b[0] + sB * far[3]);
+        L.b_dyn[N + m] = sm.stat[4][slot] + L.kmu * (b[1] + sB * far[4]);
+        L.b_dyn[2 * N + m] = sm.stat[5][slot] + L.kmu * (b[2] + sB * far[5]);
     }
 }
 
@@ -982,6 +1163,55 @@ int Surrogate::load(const char* path, cudaStream_t s) {
     pack_bf16(s);
     ready_ = true;
     return ION_OK;
+}
+
+int conv_tc_selftest(int nd, int cin, int cout, int dil, uint64_t seed, float* max_rel, cudaStream_t s) {
+    if (nd < 4 || (nd * nd * nd) % 128 != 0 || !(cin == 16 || cin == 32) || !(cout == 32 || cout == 168) ||
+        (cin == 16 && cout != 32))
+        return ION_E_INVALID;
+    const int V = nd * nd * nd, K = 27 * cin;
+    __nv_bfloat16 *act = nullptr, *w = nullptr, *ob1 = nullptr, *ob2 = nullptr;
+    float *o1 = nullptr, *o2 = nullptr;
+    uint32_t* err = nullptr;
+    bool ok = cudaMalloc(&act, (size_t)V * cin * 2) == cudaSuccess && cudaMalloc(&w, (size_t)cout * K * 2) == cudaSuccess &&
+              cudaMalloc(&o1, (size_t)cout * V * 4) == cudaSuccess && cudaMalloc(&o2, (size_t)cout * V * 4) == cudaSuccess &&
+              cudaMalloc(&ob1, (size_t)cout * V * 2) == cudaSuccess && cudaMalloc(&ob2, (size_t)cout * V * 2) == cudaSuccess &&
+              cudaMalloc(&err, 4) == cudaSuccess;
+    int rc = ok ? ION_OK : ION_E_NOMEM;
+    if (!rc) {
+        cudaMemsetAsync(err, 0, 4, s);
+        k_fill_bf16<<<blocks_for((size_t)V * cin, 256), 256, 0, s>>>(act, (size_t)V * cin, seed);
+        k_fill_bf16<<<blocks_for((size_t)cout * K, 256), 256, 0, s>>>(w, (size_t)cout * K, seed ^ 0xabcdefull);
+        const unsigned gx = blocks_for((size_t)(V / 16) * 32, 128), gt = (unsigned)(V / 128);
+        if (cin == 16) {
+            k_conv_bf16<16, 1><<<dim3(gx, cout / 8), 128, 0, s>>>(act, w, nullptr, o1, ob1, cout, dil, nd);
+            k_conv_tc<16, 32><<<gt, 128, 0, s>>>(act, w, nullptr, o2, ob2, cout, dil, nd, err);
+        } else if (cout == 32) {
+            k_conv_bf16<32, 1><<<dim3(gx, 4), 128, 0, s>>>(act, w, nullptr, o1, ob1, cout, dil, nd);
+            k_conv_tc<32, 32><<<gt, 128, 0, s>>>(act, w, nullptr, o2, ob2, cout, dil, nd, err);
+        } else {
+            k_conv_bf16<32, 1><<<dim3(gx, 21), 128, 0, s>>>(act, w, nullptr, o1, ob1, cout, dil, nd);
+            k_conv_tc<32, 176><<<gt, 128, 0, s>>>(act, w, nullptr, o2, ob2, cout, dil, nd, err);
+        }
+        std::vector<float> h1((size_t)cout * V), h2((size_t)cout * V);
+        uint32_t herr = 0;
+        cudaMemcpyAsync(h1.data(), o1, h1.size() * 4, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(h2.data(), o2, h2.size() * 4, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, s);
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) rc = ION_E_CUDA;
+        else if (herr) rc = ION_E_TIMEOUT;
+        else {
+            double dmax = 0.0, rmax = 0.0;
+            for (size_t i = 0; i < h1.size(); i++) {
+                dmax = std::max(dmax, (double)std::fabs(h1[i] - h2[i]));
+                rmax = std::max(rmax, (double)std::fabs(h1[i]));
+            }
+            *max_rel = (float)(rmax > 0.0 ? dmax / rmax : dmax);
+        }
+    }
+    cudaFree(act); cudaFree(w); cudaFree(o1); cudaFree(o2); cudaFree(ob1); cudaFree(ob2); cudaFree(err);
+    cudaGetLastError();
+    return rc;
 }
 
 }  // namespace ion

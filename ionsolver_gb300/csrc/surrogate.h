@@ -10,13 +10,16 @@
 
 namespace ion {
 
+// the tcgen05 convolution against the mma.sync one (self-test, see surrogate.cu)
+int conv_tc_selftest(int nd, int cin, int cout, int dil, uint64_t seed, float* max_rel, cudaStream_t s);
+
 class Surrogate {
 public:
     static constexpr int RNEAR = 2;           // bins within this Chebyshev distance are summed exactly
     static constexpr int NODES = 27;          // 3 x 3 x 3 interpolation nodes per block
     static constexpr int OUT_CH = NODES * 6;  // (Ex,Ey,Ez,Bx,By,Bz) per node
     static constexpr int OUT_PAD = 168;       // head channels: OUT_CH rounded up to 8 (the rest are zero)
-    static constexpr int MAX_BLOCK = 64;      // largest LOD block edge (cells) the per-cell kernel tabulates
+    static constexpr int MAX_BLOCK = 32;      // largest LOD block edge (cells) the per-cell kernel tabulates
     ~Surrogate();
     int init(int nd, float bsx, float bsy, float bsz, int first_src);
     // generates `nsamples` snapshots (random charge/current per bin, exact far-field
