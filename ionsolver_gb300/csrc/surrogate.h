@@ -74,7 +74,7 @@ private:
     size_t nw_ = 0, nwk_ = 0;
     float *w_ = nullptr, *gw_ = nullptr, *m_ = nullptr, *v_ = nullptr, *wt_ = nullptr;
     __nv_bfloat16* wk_ = nullptr;
-    float *scales_ = nullptr, *last_ = nullptr, *xin_ = nullptr, *yout_ = nullptr, *ha_ = nullptr, *hb_ = nullptr;
+    float *scales_ = nullptr, *last_ = nullptr, *xin_ = nullptr, *yout_ = nullptr, *ha_ = nullptr;
     __nv_bfloat16 *ab_ = nullptr, *bb_ = nullptr, *xb_ = nullptr;
     uint32_t *stats_ = nullptr, *flag_ = nullptr;
     unsigned long long* counters_ = nullptr;

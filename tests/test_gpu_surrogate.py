@@ -176,3 +176,18 @@ def test_save_load_roundtrip(trained, tmp_path):
     x = _sources(np.random.default_rng(4), 1)[0]
     assert np.array_equal(other.surrogate_forward(x, bf16=True), lbm.surrogate_forward(x, bf16=True))
     assert np.array_equal(other.surrogate_weights(), lbm.surrogate_weights())
+
+
+@pytest.mark.parametrize("nd,cin,cout,dil", [(16, 16, 32, 1), (16, 32, 32, 2), (16, 32, 168, 1), (8, 32, 32, 4),
+                                             (8, 32, 168, 2)])
+def test_tcgen05_convolution_matches_mma_sync(nd, cin, cout, dil):
+    """The tcgen05 implicit-GEMM convolution (TMEM accumulator, operands staged
+    in shared memory) against the mma.sync convolution on the same BF16
+    activations and weights: the same products summed in another order, so
+    max |diff| / max |out| below 1e-3 (a wrong operand layout gives O(1))."""
+    import ctypes as C
+    from ionsolver_gb300 import _native as N
+    err = C.c_float(-1.0)
+    N.check(N.lib().ion_check_tcgen05_conv(nd, cin, cout, dil, 0x5eed + nd + cin + cout + dil, C.byref(err)))
+    print(f"\ntcgen05 conv nd {nd} cin {cin} cout {cout} dil {dil}: max rel {err.value:.3e}")
+    assert 0.0 <= err.value < 1e-3
