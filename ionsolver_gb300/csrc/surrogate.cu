@@ -527,28 +527,49 @@ __global__ void k_pack_weights(const float* w, __nv_bfloat16* wkT, int cin, int 
     wkT[i] = __float2bfloat16(ci < cin ? w[((size_t)co * cin + ci) * 27 + tap] : 0.0f);
 }
 
-// scales of the current sources: max |q| and max |q v| over the bins in range
+// statistics of the current sources over the bins first..V-1: means q_m, J_m of q
+// and of q v (FP64 sums), and the largest deviations from them.  scales[0] =
+// max |q - q_m|, scales[1] = max over the three components of |q v - J_m| (1 where
+// zero), scales[2] = q_m, scales[3..5] = J_m.
 __global__ void k_source_scale(const float* qu_lod, int V, int first, float* scales) {
-    __shared__ float rq[256], rv[256];
+    __shared__ double r[4][256];
+    __shared__ float mean[4];
+    const float4* qu = (const float4*)qu_lod;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    for (int v = first + threadIdx.x; v < V; v += blockDim.x) {
+        const float4 L = qu[v];
+        s0 += L.x; s1 += L.x * L.y; s2 += L.x * L.z; s3 += L.x * L.w;
+    }
+    r[0][threadIdx.x] = s0; r[1][threadIdx.x] = s1; r[2][threadIdx.x] = s2; r[3][threadIdx.x] = s3;
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off)
+            for (int c = 0; c < 4; c++) r[c][threadIdx.x] += r[c][threadIdx.x + off];
+        __syncthreads();
+    }
+    if (threadIdx.x < 4) mean[threadIdx.x] = V > first ? (float)(r[threadIdx.x][0] / (double)(V - first)) : 0.0f;
+    __syncthreads();
     float mq = 0.0f, mv = 0.0f;
     for (int v = first + threadIdx.x; v < V; v += blockDim.x) {
-        const float4 L = ((const float4*)qu_lod)[v];
-        mq = fmaxf(mq, fabsf(L.x));
-        mv = fmaxf(mv, fmaxf(fabsf(L.x * L.y), fmaxf(fabsf(L.x * L.z), fabsf(L.x * L.w))));
+        const float4 L = qu[v];
+        mq = fmaxf(mq, fabsf(L.x - mean[0]));
+        mv = fmaxf(mv, fmaxf(fabsf(L.x * L.y - mean[1]), fmaxf(fabsf(L.x * L.z - mean[2]), fabsf(L.x * L.w - mean[3]))));
     }
-    rq[threadIdx.x] = mq;
-    rv[threadIdx.x] = mv;
+    __syncthreads();
+    r[0][threadIdx.x] = mq;
+    r[1][threadIdx.x] = mv;
     __syncthreads();
     for (int off = blockDim.x / 2; off > 0; off >>= 1) {
         if (threadIdx.x < off) {
-            rq[threadIdx.x] = fmaxf(rq[threadIdx.x], rq[threadIdx.x + off]);
-            rv[threadIdx.x] = fmaxf(rv[threadIdx.x], rv[threadIdx.x + off]);
+            r[0][threadIdx.x] = fmax(r[0][threadIdx.x], r[0][threadIdx.x + off]);
+            r[1][threadIdx.x] = fmax(r[1][threadIdx.x], r[1][threadIdx.x + off]);
         }
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        scales[0] = rq[0] > 0.0f ? rq[0] : 1.0f;
-        scales[1] = rv[0] > 0.0f ? rv[0] : 1.0f;
+        scales[0] = r[0][0] > 0.0 ? (float)r[0][0] : 1.0f;
+        scales[1] = r[1][0] > 0.0 ? (float)r[1][0] : 1.0f;
+        for (int c = 0; c < 4; c++) scales[2 + c] = mean[c];
     }
 }
 
@@ -583,10 +604,10 @@ __device__ __forceinline__ void quad_weights(float t, float* w) {  // Lagrange w
 }
 
 __device__ __forceinline__ void surrogate_tile(const DevLbm& L, SurSmem& sm, uint32_t bin, int bx, int by, int bz,
-                                               uint32_t tile, uint32_t cells, float sE, float sB);
+                                               uint32_t tile, uint32_t cells);
 
-__global__ void __launch_bounds__(SC_THREADS) k_surrogate_cells(const DevLbm L, const float* Y, const float* scales,
-                                                                float yE, float yB) {
+__global__ void __launch_bounds__(SC_THREADS) k_surrogate_cells(const DevLbm L, const float* Y, const float* G,
+                                                                const float* scales, float yE, float yB) {
     __shared__ __align__(16) SurSmem sm;
     const uint32_t bin = blockIdx.x;
     const int nd = (int)L.nd, V = nd * nd * nd;
@@ -610,7 +631,19 @@ __global__ void __launch_bounds__(SC_THREADS) k_surrogate_cells(const DevLbm L, 
         }
         if (lane == 0) sm.count = cnt;
     }
-    for (uint32_t i = threadIdx.x; i < (uint32_t)Surrogate::OUT_CH; i += blockDim.x) sm.node[i] = Y[(size_t)i * V + bin];
+    {  // node values in field units: network (fluctuations) + mean-source term
+        const float sE = scales[0] * yE, sB = scales[1] * yB, qm = scales[2];
+        const float jx = scales[3], jy = scales[4], jz = scales[5];
+        for (uint32_t i = threadIdx.x; i < (uint32_t)Surrogate::OUT_CH; i += blockDim.x) {
+            const uint32_t j6 = i - i % 6u, c = i % 6u;
+            const float y = Y[(size_t)i * V + bin];
+            const float gx = G[(size_t)j6 * V + bin], gy = G[(size_t)(j6 + 1) * V + bin], gz = G[(size_t)(j6 + 2) * V + bin];
+            float v;
+            if (c < 3u) v = fmaf(sE, y, qm * (c == 0u ? gx : c == 1u ? gy : gz));
+            else v = fmaf(sB, y, c == 3u ? jy * gz - jz * gy : c == 4u ? jz * gx - jx * gz : jx * gy - jy * gx);
+            sm.node[i] = v;
+        }
+    }
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < L.bsx * 9u * 8u; i += blockDim.x) {
         const uint32_t lx = i / 72u, jk = (i / 8u) % 9u, c = i % 8u;
@@ -624,13 +657,11 @@ __global__ void __launch_bounds__(SC_THREADS) k_surrogate_cells(const DevLbm L, 
     __syncthreads();
 
     const uint32_t cells = L.bsx * L.bsy * L.bsz;
-    const float sE = scales[0] * yE, sB = scales[1] * yB;
-    for (uint32_t tile = 0; tile * SC_CELLS < cells; tile++)
-        surrogate_tile(L, sm, bin, bx, by, bz, tile, cells, sE, sB);
+    for (uint32_t tile = 0; tile * SC_CELLS < cells; tile++) surrogate_tile(L, sm, bin, bx, by, bz, tile, cells);
 }
 
 __device__ __forceinline__ void surrogate_tile(const DevLbm& L, SurSmem& sm, uint32_t bin, int bx, int by, int bz,
-                                               uint32_t tile, uint32_t cells, float sE, float sB) {
+                                               uint32_t tile, uint32_t cells) {
     // cell k of this thread: local index li -> (lx, ly, lz) in the bin -> global (x, y, z)
     auto cell = [&](uint32_t k, uint32_t& lx, uint32_t& ly, uint32_t& lz) -> uint32_t {
         const uint32_t li = tile * SC_CELLS + threadIdx.x + k * SC_THREADS;
@@ -700,12 +731,12 @@ __device__ __forceinline__ void surrogate_tile(const DevLbm& L, SurSmem& sm, uin
             far[0] = fmaf(wgt, a.x, far[0]); far[1] = fmaf(wgt, a.y, far[1]); far[2] = fmaf(wgt, a.z, far[2]);
             far[3] = fmaf(wgt, a.w, far[3]); far[4] = fmaf(wgt, b2.x, far[4]); far[5] = fmaf(wgt, b2.y, far[5]);
         }
-        L.e_dyn[m] = sm.stat[0][slot] + L.ke * (e[0] + sE * far[0]);
-        L.e_dyn[N + m] = sm.stat[1][slot] + L.ke * (e[1] + sE * far[1]);
-        L.e_dyn[2 * N + m] = sm.stat[2][slot] + L.ke * (e[2] + sE * far[2]);
-        L.b_dyn[m] = sm.stat[3][slot] + L.kmu * (b[0] + sB * far[3]);
-        L.b_dyn[N + m] = sm.stat[4][slot] + L.kmu * (b[1] + sB * far[4]);
-        L.b_dyn[2 * N + m] = sm.stat[5][slot] + L.kmu * (b[2] + sB * far[5]);
+        L.e_dyn[m] = sm.stat[0][slot] + L.ke * (e[0] + far[0]);
+        L.e_dyn[N + m] = sm.stat[1][slot] + L.ke * (e[1] + far[1]);
+        L.e_dyn[2 * N + m] = sm.stat[2][slot] + L.ke * (e[2] + far[2]);
+        L.b_dyn[m] = sm.stat[3][slot] + L.kmu * (b[0] + far[3]);
+        L.b_dyn[N + m] = sm.stat[4][slot] + L.kmu * (b[1] + far[4]);
+        L.b_dyn[2 * N + m] = sm.stat[5][slot] + L.kmu * (b[2] + far[5]);
     }
 }
 
@@ -844,7 +875,8 @@ int Surrogate::init(int nd, float bsx, float bsy, float bsz, int first_src) {
     rc |= alloc((void**)&v_, nw_ * 4);
     rc |= alloc((void**)&wt_, (size_t)32 * OUT_PAD * 27 * 4);
     rc |= alloc((void**)&wk_, nwk_ * 2);
-    rc |= alloc((void**)&scales_, 4 * 4);
+    rc |= alloc((void**)&scales_, 8 * 4);
+    rc |= alloc((void**)&gunit_, (size_t)OUT_PAD * V_ * 4);
     rc |= alloc((void**)&stats_, 8 * 4);
     rc |= alloc((void**)&flag_, 4);
     rc |= alloc((void**)&last_, 2 * 4);
@@ -856,6 +888,15 @@ int Surrogate::init(int nd, float bsx, float bsy, float bsz, int first_src) {
     rc |= alloc((void**)&bb_, (size_t)32 * V_ * 2);
     rc |= alloc((void**)&xb_, (size_t)16 * V_ * 2);
     if (rc) return ION_E_NOMEM;
+    // far field of a unit charge in every source bin at the 27 nodes: the field of
+    // the mean sources (E = q_m G, B = J_m x G), exact and fixed by the geometry
+    {
+        std::vector<float> one((size_t)4 * V_, 0.0f);
+        for (int v = first_; v < V_; v++) one[v] = 1.0f;
+        if (cudaMemcpy(xin_, one.data(), one.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) return ION_E_CUDA;
+        k_far_targets<<<blocks_for((size_t)V_ * NODES, 256), 256>>>(xin_, nd_, bs_[0], bs_[1], bs_[2], RNEAR, gunit_, 1);
+        if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return ION_E_CUDA;
+    }
     return reset_weights(seed_);
 }
 
@@ -919,6 +960,59 @@ void Surrogate::backward_fp32(const float* X, int B, std::vector<float*>& acts, 
     g[2] = gtmp;
 }
 
+// One training snapshot of the network input, x [4][V]: the fluctuations of the bin
+// sources about their means (the means' field is exact, outside the network).
+// Each channel is a random mix of up to three plane waves of wavenumber <= 2 per
+// axis, a Gaussian charge cloud and white noise, minus its mean over the source
+// bins, then divided by its largest deviation like the inference input (charge
+// alone; current by the largest of its three components).  Bins below first_src
+// carry no sources.
+void Surrogate::make_snapshot(std::mt19937_64& gen, float* x) const {
+    std::uniform_real_distribution<float> U(-1.0f, 1.0f), P(0.0f, 1.0f);
+    std::uniform_int_distribution<int> K(0, 2);
+    const int nd = nd_;
+    const float tau = 6.28318530717958647692f;
+    for (int c = 0; c < 4; c++) {
+        float* xc = x + (size_t)c * V_;
+        const int waves = P(gen) < 0.6f ? 1 + (int)(P(gen) * 3.0f) : 0;
+        float wk[3][3], wa[3], wp[3];
+        for (int w = 0; w < waves; w++) {
+            for (int d = 0; d < 3; d++) wk[w][d] = (float)K(gen);
+            wa[w] = U(gen);
+            wp[w] = tau * P(gen);
+        }
+        const bool blob = P(gen) < 0.4f;
+        const float bc[3] = {nd * P(gen), nd * P(gen), nd * P(gen)}, bw = 1.0f + 3.0f * P(gen), ba = U(gen);
+        const float white = P(gen) < 0.3f ? 1.0f : 0.05f + 0.5f * P(gen);
+        for (int v = 0; v < V_; v++) {
+            if (v < first_) { xc[v] = 0.0f; continue; }
+            const float px = (float)(v % nd), py = (float)((v / nd) % nd), pz = (float)(v / (nd * nd));
+            float val = white * U(gen);
+            for (int w = 0; w < waves; w++)
+                val += wa[w] * std::cos(tau * (wk[w][0] * px + wk[w][1] * py + wk[w][2] * pz) / (float)nd + wp[w]);
+            if (blob) {
+                const float r2 = (px - bc[0]) * (px - bc[0]) + (py - bc[1]) * (py - bc[1]) + (pz - bc[2]) * (pz - bc[2]);
+                val += ba * std::exp(-0.5f * r2 / (bw * bw));
+            }
+            xc[v] = val;
+        }
+        double mean = 0.0;
+        for (int v = first_; v < V_; v++) mean += xc[v];
+        mean /= std::max(V_ - first_, 1);
+        for (int v = first_; v < V_; v++) xc[v] -= (float)mean;
+    }
+    float mq = 0.0f, mv = 0.0f;
+    for (int v = 0; v < V_; v++) {
+        mq = std::max(mq, std::fabs(x[v]));
+        for (int c = 1; c < 4; c++) mv = std::max(mv, std::fabs(x[(size_t)c * V_ + v]));
+    }
+    for (int v = 0; v < V_; v++) {
+        if (mq > 0.0f) x[v] /= mq;
+        for (int c = 1; c < 4; c++)
+            if (mv > 0.0f) x[(size_t)c * V_ + v] /= mv;
+    }
+}
+
 int Surrogate::train(int nsamples, int epochs, int batch, float lr, uint64_t seed, cudaStream_t s, float* rel_err) {
     // every training starts from the same initial weights (a function of the seed)
     if (int rc = reset_weights(seed ^ 0x5EEDu)) return rc;
@@ -932,11 +1026,8 @@ int Surrogate::train(int nsamples, int epochs, int batch, float lr, uint64_t see
     }
     {
         std::mt19937_64 gen(seed);
-        std::uniform_real_distribution<float> U(-1.0f, 1.0f);
         std::vector<float> h(xs * nsamples);
-        for (int sidx = 0; sidx < nsamples; sidx++)
-            for (int c = 0; c < 4; c++)
-                for (int v = 0; v < V_; v++) h[sidx * xs + c * V_ + v] = v >= first_ ? U(gen) : 0.0f;
+        for (int sidx = 0; sidx < nsamples; sidx++) make_snapshot(gen, h.data() + sidx * xs);
         cudaMemcpy(X, h.data(), h.size() * 4, cudaMemcpyHostToDevice);
     }
     cudaMemsetAsync(T, 0, ys * nsamples * 4, s);  // padding channels stay zero
@@ -1074,23 +1165,24 @@ void Surrogate::step(const DevLbm& L, cudaStream_t s, uint32_t salt) {
     k_source_scale<<<1, 256, 0, s>>>(L.qu_lod, V_, first_, scales_);
     k_pack_input_dev(L, s);
     infer_bf16(xin_, s);
-    k_surrogate_cells<<<L.n_bins, SC_THREADS, 0, s>>>(L, yout_, scales_, yE_, yB_);
+    k_surrogate_cells<<<L.n_bins, SC_THREADS, 0, s>>>(L, yout_, gunit_, scales_, yE_, yB_);
     k_sample_check<<<blocks_for((size_t)check_cells_ * 32, 128), 128, 0, s>>>(L, check_cells_, salt, stats_, counters_);
     k_sample_decide<<<1, 1, 0, s>>>(stats_, tol_, flag_, last_, counters_);
 }
 
-// network input from the LOD table: X[c][v] = (q, q vx, q vy, q vz) divided by
-// the step's source scales; bins below first_src are no sources (sim_kernels.cl:943)
+// network input from the LOD table: X[c][v] = (q - q_m, q vx - J_m,x, q vy - J_m,y,
+// q vz - J_m,z) divided by the step's deviation scales (the fluctuations about the
+// source means); bins below first_src are no sources (sim_kernels.cl:943)
 __global__ void k_pack_input_scaled(const float* qu_lod, int V, int first, const float* scales, float* X) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= V) return;
     const float4 L = ((const float4*)qu_lod)[v];
     const bool use = v >= first;
     const float sq = scales[0], sv = scales[1];
-    X[v] = use ? L.x / sq : 0.0f;
-    X[V + v] = use ? L.x * L.y / sv : 0.0f;
-    X[2 * V + v] = use ? L.x * L.z / sv : 0.0f;
-    X[3 * V + v] = use ? L.x * L.w / sv : 0.0f;
+    X[v] = use ? (L.x - scales[2]) / sq : 0.0f;
+    X[V + v] = use ? (L.x * L.y - scales[3]) / sv : 0.0f;
+    X[2 * V + v] = use ? (L.x * L.z - scales[4]) / sv : 0.0f;
+    X[3 * V + v] = use ? (L.x * L.w - scales[5]) / sv : 0.0f;
 }
 
 void Surrogate::k_pack_input_dev(const DevLbm& L, cudaStream_t s) {

@@ -1,6 +1,7 @@
 // surrogate.h -- the learned far field of the E/B update (surrogate.cu).
 #pragma once
 #include <cstdint>
+#include <random>
 #include <vector>
 
 #include <cuda_bf16.h>
@@ -66,6 +67,7 @@ private:
     void backward_fp32(const float* X, int B, std::vector<float*>& acts, const float* gY, std::vector<float*>& g,
                        cudaStream_t s);
     void pack_bf16(cudaStream_t s);
+    void make_snapshot(std::mt19937_64& gen, float* x) const;
     void k_pack_input_dev(const DevLbm& L, cudaStream_t s);
 
     int nd_ = 0, V_ = 0, first_ = 0;
@@ -75,6 +77,7 @@ private:
     float *w_ = nullptr, *gw_ = nullptr, *m_ = nullptr, *v_ = nullptr, *wt_ = nullptr;
     __nv_bfloat16* wk_ = nullptr;
     float *scales_ = nullptr, *last_ = nullptr, *xin_ = nullptr, *yout_ = nullptr, *ha_ = nullptr;
+    float* gunit_ = nullptr;  // far field of unit sources in every source bin, [OUT_PAD][V]
     __nv_bfloat16 *ab_ = nullptr, *bb_ = nullptr, *xb_ = nullptr;
     uint32_t *stats_ = nullptr, *flag_ = nullptr;
     unsigned long long* counters_ = nullptr;

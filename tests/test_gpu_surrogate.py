@@ -3,9 +3,10 @@
 
 Tolerances: FP32 kernels (targets, forward, gradient) 1e-4 relative to the
 float64 oracle; BF16 tensor-core forward 3e-2 relative to the FP32 forward;
-a trained network's E field after one step at most 60% of the error of the
-near-bins-only truncation (the "gain"), with the sampled check and exact
-fallback reproducing the exact FAST field bit for bit."""
+a trained network's E field after one step at most 35% of the error of the
+same path without the network (near bins exact plus the exact field of the
+mean sources: the "gain"), with the sampled check and exact fallback
+reproducing the exact FAST field bit for bit."""
 import numpy as np
 import pytest
 
@@ -110,7 +111,7 @@ def _exact_step():
     return _dyn(g)
 
 
-def test_field_gain_over_near_only(trained):
+def test_field_gain_over_no_network(trained):
     lbm, _ = trained
     e_x, b_x = _exact_step()
     w = lbm.surrogate_weights()
@@ -124,7 +125,7 @@ def test_field_gain_over_near_only(trained):
     st = lbm.surrogate_stats()
     assert st["checks"] >= 1 and st["fallbacks"] == 0 and st["nonfinite"] == 0
     assert 0.0 < st["err_e"] < 1.0 and st["err_b"] < 1e-6
-    # near bins only: the same path with a zero network
+    # without the network: near bins and the mean sources' field only (zero weights)
     lbm.surrogate_weights(np.zeros_like(w))
     _restart(lbm)
     lbm.do_time_step()
@@ -132,7 +133,8 @@ def test_field_gain_over_near_only(trained):
     e_t, _ = _dyn(lbm)
     err_t = U.rel_err(e_t, e_x)
     lbm.surrogate_weights(w)
-    assert err_s < 0.6 * err_t, (err_s, err_t)
+    print(f"\nE after one step: surrogate {err_s:.3e}, without the network {err_t:.3e}")
+    assert err_s < 0.35 * err_t, (err_s, err_t)
 
 
 def test_fallback_reproduces_exact_field(trained):
