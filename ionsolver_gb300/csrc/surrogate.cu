@@ -589,7 +589,19 @@ struct SurSmem {
     float4 t1[Surrogate::MAX_BLOCK][9][2];
     // E_stat, B_stat of the tile's cells, fetched with cp.async while the near sums run
     float stat[6][SC_CELLS];
+    // interpolation weights along y (wyz[0][ly]) and z (wyz[1][lz]) of the nodes 0, 1/2, 1
+    float4 wyz[2][Surrogate::MAX_BLOCK];
     uint32_t count;
+};
+
+// n / d for the cell indices of a bin (n < 32768, d <= 1024): floor(n m / 2^32) with
+// m = floor((2^32 - 1) / d) + 1.  With n = q d + r, n m / 2^32 = n / d + n e / 2^32,
+// 0 <= e < 1, and n e / 2^32 < n / 2^32 < 1 / d whenever n d < 2^32, so the floor is q
+// (division by invariant integers, Granlund & Montgomery 1994)
+struct Magic {
+    uint32_t d, m;
+    __device__ explicit Magic(uint32_t dd) : d(dd), m(dd > 1u ? 0xFFFFFFFFu / dd + 1u : 0u) {}
+    __device__ __forceinline__ uint32_t div(uint32_t n) const { return d > 1u ? __umulhi(n, m) : n; }
 };
 
 __device__ __forceinline__ void cp_async4(float* dst, const float* src) {
@@ -604,11 +616,12 @@ __device__ __forceinline__ void quad_weights(float t, float* w) {  // Lagrange w
 }
 
 __device__ __forceinline__ void surrogate_tile(const DevLbm& L, SurSmem& sm, uint32_t bin, int bx, int by, int bz,
-                                               uint32_t tile, uint32_t cells);
+                                               uint32_t tile, uint32_t cells, const Magic& mx, const Magic& mxy);
 
 __global__ void __launch_bounds__(SC_THREADS) k_surrogate_cells(const DevLbm L, const float* Y, const float* G,
                                                                 const float* scales, float yE, float yB) {
-    __shared__ __align__(16) SurSmem sm;
+    extern __shared__ __align__(16) uint8_t sur_smem[];  // sizeof(SurSmem), above the 48 KB of static shared memory
+    SurSmem& sm = *reinterpret_cast<SurSmem*>(sur_smem);
     const uint32_t bin = blockIdx.x;
     const int nd = (int)L.nd, V = nd * nd * nd;
     const int bx = (int)bin % nd, by = ((int)bin / nd) % nd, bz = (int)bin / (nd * nd);
@@ -654,34 +667,40 @@ __global__ void __launch_bounds__(SC_THREADS) k_surrogate_cells(const DevLbm L, 
             for (int ix = 0; ix < 3; ix++) v = fmaf(wx[ix], sm.node[(ix + 3 * jk) * 6 + c], v);
         ((float*)&sm.t1[lx][jk][0])[c] = v;
     }
+    for (uint32_t i = threadIdx.x; i < 2u * Surrogate::MAX_BLOCK; i += blockDim.x) {
+        const uint32_t a = i / Surrogate::MAX_BLOCK, l = i % Surrogate::MAX_BLOCK, b = a == 0u ? L.bsy : L.bsz;
+        float w[3];
+        quad_weights(b > 1u ? (float)l / (float)(b - 1u) : 0.0f, w);
+        sm.wyz[a][l] = make_float4(w[0], w[1], w[2], 0.0f);
+    }
     __syncthreads();
 
     const uint32_t cells = L.bsx * L.bsy * L.bsz;
-    for (uint32_t tile = 0; tile * SC_CELLS < cells; tile++) surrogate_tile(L, sm, bin, bx, by, bz, tile, cells);
+    const Magic mx(L.bsx), mxy(L.bsx * L.bsy);
+    for (uint32_t tile = 0; tile * SC_CELLS < cells; tile++) surrogate_tile(L, sm, bin, bx, by, bz, tile, cells, mx, mxy);
 }
 
 __device__ __forceinline__ void surrogate_tile(const DevLbm& L, SurSmem& sm, uint32_t bin, int bx, int by, int bz,
-                                               uint32_t tile, uint32_t cells) {
-    // cell k of this thread: local index li -> (lx, ly, lz) in the bin -> global (x, y, z)
-    auto cell = [&](uint32_t k, uint32_t& lx, uint32_t& ly, uint32_t& lz) -> uint32_t {
-        const uint32_t li = tile * SC_CELLS + threadIdx.x + k * SC_THREADS;
-        const uint32_t lc = li < cells ? li : 0u;
-        lx = lc % L.bsx; ly = (lc / L.bsx) % L.bsy; lz = lc / (L.bsx * L.bsy);
-        return li;
-    };
+                                               uint32_t tile, uint32_t cells, const Magic& mx, const Magic& mxy) {
+    // cell k of this thread: local index li -> (lx, ly, lz) in the bin, kept packed
+    // (10 bits each) for the tail; flags are read now and used after the near sums
     float rx[SC_CPT], ry[SC_CPT], rz[SC_CPT];  // cell coordinates relative to the bin centre
     FarSums fs[SC_CPT / 2];
-    uint32_t live = 0u;  // bit k: cell k exists and is not solid
+    uint32_t pc[SC_CPT], fl[SC_CPT];
     const size_t N = L.n;
     const float4 o = L.lod_pos[bin];
 #pragma unroll
     for (uint32_t k = 0; k < SC_CPT; k++) {
-        uint32_t lx, ly, lz;
-        const uint32_t li = cell(k, lx, ly, lz);
+        const uint32_t li = tile * SC_CELLS + threadIdx.x + k * SC_THREADS;
+        const bool in = li < cells;
+        const uint32_t lc = in ? li : 0u;
+        const uint32_t lz = mxy.div(lc), r = lc - lz * mxy.d, ly = mx.div(r), lx = r - ly * mx.d;
+        pc[k] = lx | ly << 10 | lz << 20;
         const uint32_t x = bx * L.bsx + lx, y = by * L.bsy + ly, z = bz * L.bsz + lz;
         const uint32_t m = x + (y + z * L.ny) * L.nx;
-        if (li < cells && (L.flags[m] & F_BO) != F_S) {
-            live |= 1u << k;
+        fl[k] = F_S;
+        if (in) {
+            fl[k] = L.flags[m];
             // the static fields are needed after the near sums: copy them into this
             // thread's shared-memory slots now (only this thread reads them)
             const uint32_t slot = k * SC_THREADS + threadIdx.x;
@@ -712,21 +731,19 @@ __device__ __forceinline__ void surrogate_tile(const DevLbm& L, SurSmem& sm, uin
     asm volatile("cp.async.commit_group;\n cp.async.wait_group 0;" ::: "memory");
 #pragma unroll
     for (uint32_t k = 0; k < SC_CPT; k++) {
-        if (!(live & (1u << k))) continue;
-        uint32_t lx, ly, lz;
-        cell(k, lx, ly, lz);
+        if ((fl[k] & F_BO) == F_S) continue;  // solid, or no cell
+        const uint32_t lx = pc[k] & 1023u, ly = (pc[k] >> 10) & 1023u, lz = pc[k] >> 20;
         const uint32_t slot = k * SC_THREADS + threadIdx.x;
         const uint32_t m = (bx * L.bsx + lx) + ((by * L.bsy + ly) + (bz * L.bsz + lz) * L.ny) * L.nx;
         float e[3] = {0.0f, 0.0f, 0.0f}, b[3] = {0.0f, 0.0f, 0.0f};
         far_finish(cp[k / 2], fs[k / 2], (k & 1u) != 0, e, b);
         // triquadratic interpolation: the x contraction is tabulated per bin (t1)
-        float wy[3], wz[3];
-        quad_weights(L.bsy > 1 ? (float)ly / (float)(L.bsy - 1) : 0.0f, wy);
-        quad_weights(L.bsz > 1 ? (float)lz / (float)(L.bsz - 1) : 0.0f, wz);
+        const float4 wy = sm.wyz[0][ly], wz = sm.wyz[1][lz];
+        const float wy3[3] = {wy.x, wy.y, wy.z}, wz3[3] = {wz.x, wz.y, wz.z};
         float far[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll
         for (int jk = 0; jk < 9; jk++) {
-            const float wgt = wy[jk % 3] * wz[jk / 3];
+            const float wgt = wy3[jk % 3] * wz3[jk / 3];
             const float4 a = sm.t1[lx][jk][0], b2 = sm.t1[lx][jk][1];
             far[0] = fmaf(wgt, a.x, far[0]); far[1] = fmaf(wgt, a.y, far[1]); far[2] = fmaf(wgt, a.z, far[2]);
             far[3] = fmaf(wgt, a.w, far[3]); far[4] = fmaf(wgt, b2.x, far[4]); far[5] = fmaf(wgt, b2.y, far[5]);
@@ -888,6 +905,9 @@ int Surrogate::init(int nd, float bsx, float bsy, float bsz, int first_src) {
     rc |= alloc((void**)&bb_, (size_t)32 * V_ * 2);
     rc |= alloc((void**)&xb_, (size_t)16 * V_ * 2);
     if (rc) return ION_E_NOMEM;
+    if (cudaFuncSetAttribute(k_surrogate_cells, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SurSmem)) !=
+        cudaSuccess)
+        return ION_E_CUDA;
     // far field of a unit charge in every source bin at the 27 nodes: the field of
     // the mean sources (E = q_m G, B = J_m x G), exact and fixed by the geometry
     {
@@ -1165,7 +1185,7 @@ void Surrogate::step(const DevLbm& L, cudaStream_t s, uint32_t salt) {
     k_source_scale<<<1, 256, 0, s>>>(L.qu_lod, V_, first_, scales_);
     k_pack_input_dev(L, s);
     infer_bf16(xin_, s);
-    k_surrogate_cells<<<L.n_bins, SC_THREADS, 0, s>>>(L, yout_, gunit_, scales_, yE_, yB_);
+    k_surrogate_cells<<<L.n_bins, SC_THREADS, sizeof(SurSmem), s>>>(L, yout_, gunit_, scales_, yE_, yB_);
     k_sample_check<<<blocks_for((size_t)check_cells_ * 32, 128), 128, 0, s>>>(L, check_cells_, salt, stats_, counters_);
     k_sample_decide<<<1, 1, 0, s>>>(stats_, tol_, flag_, last_, counters_);
 }
