@@ -30,6 +30,7 @@
 #include <cuda_bf16.h>
 
 #include "field_kernels.cuh"
+#include "tcgen05.cuh"
 #include "ion_launch.h"
 #include "surrogate.h"
 
@@ -307,30 +308,6 @@ __global__ void __launch_bounds__(128) k_conv_bf16(const __nv_bfloat16* act, con
 // lanes 32w..32w+31 = voxels), adds the residual and writes FP32 and BF16.
 // Waits are bounded; a timeout sets *err and the CTA still frees its TMEM.
 // ---------------------------------------------------------------------------
-namespace tc {
-__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-// shared-memory matrix descriptor: start >> 4 [0,14), LBO >> 4 [16,30), SBO >> 4 [32,46),
-// version 1 [46,48), base offset 0, layout SWIZZLE_NONE (0) [61,64)
-__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
-           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
-}
-// instruction descriptor, kind::f16: D F32 [4,6) = 1, A BF16 [7,10) = 1, B BF16 [10,13) = 1,
-// A and B K-major (bits 15, 16 = 0), N >> 3 [17,23), M >> 4 [24,29)
-__host__ __device__ constexpr uint32_t idesc_bf16(uint32_t m, uint32_t n) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
-}
-__device__ __forceinline__ bool wait(uint64_t* bar, uint32_t parity) {
-    for (uint32_t i = 0; i < (1u << 24); i++) {
-        uint32_t done;
-        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-                     : "=r"(done) : "r"(saddr(bar)), "r"(parity) : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-}  // namespace tc
-
 __device__ __forceinline__ void cp_async16(void* dst, const void* src, uint32_t bytes) {  // bytes 0: zero fill
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(tc::saddr(dst)), "l"(src), "r"(bytes)
                  : "memory");
@@ -618,7 +595,7 @@ __device__ __forceinline__ void quad_weights(float t, float* w) {  // Lagrange w
 __device__ __forceinline__ void surrogate_tile(const DevLbm& L, SurSmem& sm, uint32_t bin, int bx, int by, int bz,
                                                uint32_t tile, uint32_t cells, const Magic& mx, const Magic& mxy);
 
-__global__ void __launch_bounds__(SC_THREADS) k_surrogate_cells(const DevLbm L, const float* Y, const float* G,
+__global__ void __launch_bounds__(SC_THREADS, 3) k_surrogate_cells(const DevLbm L, const float* Y, const float* G,
                                                                 const float* scales, float yE, float yB) {
     extern __shared__ __align__(16) uint8_t sur_smem[];  // sizeof(SurSmem), above the 48 KB of static shared memory
     SurSmem& sm = *reinterpret_cast<SurSmem*>(sur_smem);
