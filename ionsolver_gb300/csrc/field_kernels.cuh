@@ -135,33 +135,7 @@ static __global__ void __launch_bounds__(LB_THREADS) k_lod_bins(const DevLbm L) 
 // bulk asynchronous copy global -> shared, completion counted on an mbarrier
 // (PTX ISA: cp.async.bulk, mbarrier.*; sm_90 and later)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                 ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
-}
-// Waits for the phase with the given parity; gives up after `limit` polls
-// and returns false (the caller records the failure and skips the tile).
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
-    for (uint32_t i = 0; i < limit; i++) {
-        uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done) : "r"(smem_addr(bar)), "r"(parity) : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
 constexpr uint32_t SRC_CHUNK = 256;  // sources per shared-memory tile
-constexpr uint32_t WAIT_LIMIT = 1u << 24;
 
 template <bool FAST>
 __device__ __forceinline__ void add_src(float rx, float ry, float rz, float4 val, float* e, float* b) {

@@ -235,9 +235,9 @@ int lbm_mode(const ion_config& c) { return c.ext_magneto_hydro ? (c.ext_subgrid_
 int launch_stream_collide(ion_lbm* h, uint64_t t) {
     const int ft = h->cfg.float_type, mode = lbm_mode(h->cfg);
     const bool trt = h->cfg.relaxation_time == ION_TRT;
-    if (h->q == 19) q19_stream_collide(h->L, ft, mode, trt, t, h->stream);
-    else if (h->q == 15) q15_stream_collide(h->L, ft, mode, trt, t, h->stream);
-    else q9_stream_collide(h->L, ft, mode, trt, t, h->stream);
+    if (h->q == 19) q19_stream_collide(h->L, ft, mode, trt, t, h->d_err, h->stream);
+    else if (h->q == 15) q15_stream_collide(h->L, ft, mode, trt, t, h->d_err, h->stream);
+    else q9_stream_collide(h->L, ft, mode, trt, t, h->d_err, h->stream);
     g_launches++;
     CKL();
     return ION_OK;

@@ -135,24 +135,54 @@ __host__ __device__ __forceinline__ float fp16c_decode(uint16_t x) {
     return bitsf(out);
 }
 
+// shared memory, mbarriers and bulk asynchronous copies (cp.async.bulk, completion
+// counted in bytes on an mbarrier)
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+// Waits for the phase with the given parity; gives up after `limit` polls
+// and returns false (the caller records the failure and skips the tile).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
+    for (uint32_t i = 0; i < limit; i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+constexpr uint32_t WAIT_LIMIT = 1u << 24;  // polls before a wait gives up
+
 template <int FT> struct Ddf;
 template <> struct Ddf<ION_FP32> {
     using T = float;
+    __device__ __forceinline__ static float dec(float v) { return v; }
     __device__ __forceinline__ static float ld(const float* p, size_t i) { return p[i]; }
     __device__ __forceinline__ static void st(float* p, size_t i, float x) { p[i] = x; }
 };
 template <> struct Ddf<ION_FP16S> {
     using T = uint16_t;
-    __device__ __forceinline__ static float ld(const uint16_t* p, size_t i) {
-        return __half2float(__ushort_as_half(p[i])) * 3.0517578E-5f;
-    }
+    __device__ __forceinline__ static float dec(uint16_t v) { return __half2float(__ushort_as_half(v)) * 3.0517578E-5f; }
+    __device__ __forceinline__ static float ld(const uint16_t* p, size_t i) { return dec(p[i]); }
     __device__ __forceinline__ static void st(uint16_t* p, size_t i, float x) {
         p[i] = __half_as_ushort(__float2half_rn(x * 32768.0f));
     }
 };
 template <> struct Ddf<ION_FP16C> {
     using T = uint16_t;
-    __device__ __forceinline__ static float ld(const uint16_t* p, size_t i) { return fp16c_decode(p[i]); }
+    __device__ __forceinline__ static float dec(uint16_t v) { return fp16c_decode(v); }
+    __device__ __forceinline__ static float ld(const uint16_t* p, size_t i) { return dec(p[i]); }
     __device__ __forceinline__ static void st(uint16_t* p, size_t i, float x) { p[i] = fp16c_encode(x); }
 };
 

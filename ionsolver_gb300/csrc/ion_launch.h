@@ -58,7 +58,8 @@ cudaError_t launch_batch_step(const BatchDev& B, int ft, bool mhd, bool fast, ui
 
 // per velocity set (lbm_q19.cu, lbm_q15.cu, lbm_q9.cu)
 #define ION_DECLARE_LBM_DISPATCH(NAME)                                                                    \
-    void NAME##_stream_collide(const DevLbm& L, int ft, int mode, bool trt, uint64_t t, cudaStream_t s);  \
+    void NAME##_stream_collide(const DevLbm& L, int ft, int mode, bool trt, uint64_t t, uint32_t* err,       \
+                               cudaStream_t s);                                                            \
     void NAME##_initialize(const DevLbm& L, int ft, int mode, cudaStream_t s);                            \
     void NAME##_update_fields(const DevLbm& L, int ft, uint64_t t, cudaStream_t s);
 ION_DECLARE_LBM_DISPATCH(q19)

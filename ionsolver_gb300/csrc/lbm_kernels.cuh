@@ -9,6 +9,8 @@
 // float atomics per cell, each cell stores its velocity contribution and a
 // separate pass (field_kernels.cu) sums every bin in ascending cell order.
 #pragma once
+#include <algorithm>
+
 #include "ion_device.cuh"
 #include "ion_launch.h"
 
@@ -156,6 +158,51 @@ struct Nb7 {  // D3Q7 subset (sim_kernels.cl:382-389)
     }
 };
 
+// Where sc_cell reads a cell's inputs.  Both sources return the same values, so
+// the arithmetic (and its results) do not depend on the choice.
+enum { LAT_FI = 0, LAT_EI = 1, LAT_FQI = 2 };
+// straight from global memory (Esoteric-Pull addressing, sim_kernels.cl:234-247)
+struct GlobalSrc {
+    static constexpr bool prefetch = true;
+    __device__ __forceinline__ uint8_t flags(const DevLbm& L, uint32_t n) const { return L.flags[n]; }
+    // c = 0..2: B_dyn x, y, z; 3..5: E_dyn x, y, z
+    __device__ __forceinline__ float eb(const DevLbm& L, int c, uint32_t n) const {
+        return c < 3 ? L.b_dyn[(size_t)c * L.n + n] : L.e_dyn[(size_t)(c - 3) * L.n + n];
+    }
+    template <class D, int Q, class NB>
+    __device__ __forceinline__ void load(const typename D::T* f, uint32_t N, uint32_t n, bool odd, const NB& j,
+                                         float* v, int) const {
+        ep_load<D, Q>(f, N, n, odd, j, v);
+    }
+};
+// D3Q19 offsets (in rows) of the staged streams of each lattice: fi 19, ei 19, fqi 7
+__host__ __device__ constexpr uint32_t row_stream_base(int lat) { return lat == LAT_FI ? 0u : lat == LAT_EI ? 19u : 38u; }
+// From one x-row staged in shared memory by k_sc_rows: stream s of a lattice holds
+// the row that DDF s of every cell of the row is read from (stream 0 and the odd
+// streams: the cell's own row; stream i + 1: the row of the neighbour in direction i,
+// read at the neighbour's x), then the E/B rows and the flags row.
+template <class T>
+struct RowSrc {
+    static constexpr bool prefetch = false;
+    const uint8_t* buf;
+    uint32_t nx, x, xp, xm, eb_off, fl_off;
+    __device__ __forceinline__ uint8_t flags(const DevLbm&, uint32_t) const { return buf[fl_off + x]; }
+    __device__ __forceinline__ float eb(const DevLbm&, int c, uint32_t) const {
+        return reinterpret_cast<const float*>(buf + eb_off)[(uint32_t)c * nx + x];
+    }
+    template <class D, int Q, class NB>
+    __device__ __forceinline__ void load(const T*, uint32_t, uint32_t, bool, const NB&, float* v, int lat) const {
+        const T* r = reinterpret_cast<const T*>(buf) + row_stream_base(lat) * nx;
+        v[0] = D::dec(r[x]);
+#pragma unroll
+        for (int i = 1; i < Q; i += 2) {
+            const int cx = Q == 7 ? (i == 1 ? 1 : 0) : VSet<19>::c(i, 0);
+            v[i] = D::dec(r[(uint32_t)i * nx + x]);
+            v[i + 1] = D::dec(r[(uint32_t)(i + 1) * nx + (cx > 0 ? xp : cx < 0 ? xm : x)]);
+        }
+    }
+};
+
 // ---------------------------------------------------------------------------
 // Fused equilibrium / forcing / collision / store, one direction pair at a
 // time.  Each value is computed with exactly the operations of
@@ -269,14 +316,14 @@ __device__ __forceinline__ float mag_v(const float* V, size_t N, uint32_t m) {
     return sqrtf((V[m] * V[m] + V[N + m] * V[N + m]) + V[2 * N + m] * V[2 * N + m]);
 }
 
-template <int Q, int FT, bool MHD, bool TRT, bool ECR = false>
-__device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const bool odd) {
+template <int Q, int FT, bool MHD, bool TRT, bool ECR = false, class SRC = GlobalSrc>
+__device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const bool odd, const SRC& S = SRC{}) {
     using V = VSet<Q>;
     using D = Ddf<FT>;
     using T = typename D::T;
     const uint32_t N = L.n;
     {
-        const uint8_t fbo = L.flags[n] & F_BO;
+        const uint8_t fbo = S.flags(L, n) & F_BO;
         if (fbo == F_S) return;
         const bool eqc = L.ext_eq && fbo == F_E;
         uint32_t x, y, z;
@@ -291,13 +338,15 @@ __device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const
         float rhoe = 0.0f, Bx = 0.0f, By = 0.0f, Bz = 0.0f, Ex = 0.0f, Ey = 0.0f, Ez = 0.0f, dq_ecr = 0.0f;
         if constexpr (MHD) {
             // the gas and charge lattices are read after the electron gas: start them towards L2
-            ep_prefetch<T, Q>((const T*)L.fi, N, n, odd, j);
-            ep_prefetch<T, 7>((const T*)L.fqi, N, n, odd, Nb7{nb});
-            Bx = L.b_dyn[n]; By = L.b_dyn[(size_t)N + n]; Bz = L.b_dyn[2 * (size_t)N + n];
-            Ex = L.e_dyn[n]; Ey = L.e_dyn[(size_t)N + n]; Ez = L.e_dyn[2 * (size_t)N + n];
+            if constexpr (SRC::prefetch) {
+                ep_prefetch<T, Q>((const T*)L.fi, N, n, odd, j);
+                ep_prefetch<T, 7>((const T*)L.fqi, N, n, odd, Nb7{nb});
+            }
+            Bx = S.eb(L, 0, n); By = S.eb(L, 1, n); Bz = S.eb(L, 2, n);
+            Ex = S.eb(L, 3, n); Ey = S.eb(L, 4, n); Ez = S.eb(L, 5, n);
             // electron gas: moments, Lorentz force, Guo half-step, SRT, store
             float ehn[Q];
-            ep_load<D, Q>((const T*)L.ei, N, n, odd, j, ehn);
+            S.template load<D, Q>((const T*)L.ei, N, n, odd, j, ehn, LAT_EI);
             float uxe, uye, uze;
             moments<V>(ehn, rhoe, uxe, uye, uze);
             if constexpr (ECR) {  // SUBGRID_ECR, sim_kernels.cl:564-628 (the ionisation term is the reference's placeholder)
@@ -350,7 +399,7 @@ __device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const
             srt_store<V, D>((T*)L.ei, N, n, odd, j, ehn, ee, fe, true, c_tau, w, eqc);
         }
         float fhn[Q];
-        ep_load<D, Q>((const T*)L.fi, N, n, odd, j, fhn);
+        S.template load<D, Q>((const T*)L.fi, N, n, odd, j, fhn, LAT_FI);
         float rhon, uxn, uyn, uzn;
         if (eqc) { rhon = L.rho[n]; uxn = L.u[n]; uyn = L.u[(size_t)N + n]; uzn = L.u[2 * (size_t)N + n]; }
         else moments<V>(fhn, rhon, uxn, uyn, uzn);
@@ -364,7 +413,7 @@ __device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const
             float rhoq;
             {
                 float qhn[7];
-                ep_load<D, 7>((const T*)L.fqi, N, n, odd, j7, qhn);
+                S.template load<D, 7>((const T*)L.fqi, N, n, odd, j7, qhn, LAT_FQI);
                 rhoq = 0.0f;
 #pragma unroll
                 for (int i = 0; i < 7; i++) rhoq = rhoq + qhn[i];
@@ -415,6 +464,131 @@ __global__ void __launch_bounds__(256, MHD ? 2 : 4) k_stream_collide(const DevLb
     const bool odd = odd_t != 0u;
     for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < L.n; n += gridDim.x * blockDim.x)
         sc_cell<Q, FT, MHD, TRT, ECR>(L, n, odd);
+}
+
+// ---------------------------------------------------------------------------
+// D3Q19 stream_collide over x-rows staged in shared memory.  Each CTA walks rows
+// (y, z) = blockIdx.x, blockIdx.x + gridDim.x, ...; for the next row one thread
+// issues bulk asynchronous copies (cp.async.bulk, completion on the buffer's
+// mbarrier) of every stream the row's cells read -- per lattice the own-row slot of
+// DDF 0 and of each odd direction, and for each even direction the slot row of the
+// neighbour in the pair's direction (periodic in y and z; the x shift is applied
+// when reading) -- plus the E/B and flag rows, while the CTA computes the current
+// row from the other buffer.  All streams are contiguous rows, so the copies keep
+// tens of KB per SM in flight without holding registers.  In Esoteric-Pull every
+// slot is read and written by the same cell within a step, so staging a row ahead
+// of its cells' stores is safe.  The arithmetic is sc_cell's (RowSrc only changes
+// where values are read); stores go to global memory as before.  A copy that does
+// not land within the wait limit sets *err and the CTA stops after waiting (bounded)
+// for its copies in flight.
+// ---------------------------------------------------------------------------
+template <int FT, bool MHD>
+__host__ __device__ constexpr uint32_t row_streams() { return MHD ? 45u : 19u; }
+
+template <int FT, bool MHD>
+__host__ __device__ inline uint32_t row_bytes(uint32_t nx) {
+    using T = typename Ddf<FT>::T;
+    return row_streams<FT, MHD>() * nx * (uint32_t)sizeof(T) + (MHD ? 6u * nx * 4u : 0u) + ((nx + 15u) & ~15u);
+}
+
+template <int FT, bool MHD, bool TRT>
+__global__ void __launch_bounds__(256, 2) k_sc_rows(const DevLbm L, const uint32_t odd_t, uint32_t* err) {
+    using V = VSet<19>;
+    using T = typename Ddf<FT>::T;
+    extern __shared__ __align__(128) uint8_t rows_smem[];
+    __shared__ __align__(8) uint64_t bar[2];
+    const bool odd = odd_t != 0u;
+    const uint32_t nx = L.nx, ny = L.ny, nz = L.nz, nrows = ny * nz, N = L.n;
+    const uint32_t rb = nx * (uint32_t)sizeof(T), RB = row_bytes<FT, MHD>(nx);
+    const uint32_t eb_off = row_streams<FT, MHD>() * rb, fl_off = eb_off + (MHD ? 6u * nx * 4u : 0u);
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1u);
+        mbar_init(&bar[1], 1u);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    // copies of row r into buffer b (one thread)
+    auto stage = [&](uint32_t r, uint32_t b) {
+        uint8_t* dst = rows_smem + b * RB;
+        const uint32_t y = r % ny, z = r / ny;
+        const uint32_t own = (y + z * ny) * nx;
+        mbar_expect_tx(&bar[b], RB);
+        auto lattice = [&](const T* f, uint32_t base, int Q) {
+            bulk_g2s(dst + base * rb, f + own, rb, &bar[b]);
+            for (int i = 1; i < Q; i += 2) {
+                const int cy = Q == 7 ? (i == 3 ? 1 : 0) : V::c(i, 1), cz = Q == 7 ? (i == 5 ? 1 : 0) : V::c(i, 2);
+                const uint32_t yy = cy > 0 ? (y + 1u == ny ? 0u : y + 1u) : cy < 0 ? (y == 0u ? ny - 1u : y - 1u) : y;
+                const uint32_t zz = cz > 0 ? (z + 1u == nz ? 0u : z + 1u) : cz < 0 ? (z == 0u ? nz - 1u : z - 1u) : z;
+                const uint32_t s_own = odd ? (uint32_t)i : (uint32_t)i + 1u, s_nbr = odd ? (uint32_t)i + 1u : (uint32_t)i;
+                bulk_g2s(dst + (base + i) * rb, f + (size_t)s_own * N + own, rb, &bar[b]);
+                bulk_g2s(dst + (base + i + 1) * rb, f + (size_t)s_nbr * N + (yy + zz * ny) * nx, rb, &bar[b]);
+            }
+        };
+        lattice((const T*)L.fi, row_stream_base(LAT_FI), 19);
+        if constexpr (MHD) {
+            lattice((const T*)L.ei, row_stream_base(LAT_EI), 19);
+            lattice((const T*)L.fqi, row_stream_base(LAT_FQI), 7);
+            for (uint32_t c = 0; c < 3; c++) {
+                bulk_g2s(dst + eb_off + c * nx * 4u, L.b_dyn + (size_t)c * N + own, nx * 4u, &bar[b]);
+                bulk_g2s(dst + eb_off + (3u + c) * nx * 4u, L.e_dyn + (size_t)c * N + own, nx * 4u, &bar[b]);
+            }
+        }
+        bulk_g2s(dst + fl_off, L.flags + own, (nx + 15u) & ~15u, &bar[b]);
+    };
+    uint32_t k = 0;
+    bool ok = true;
+    if (threadIdx.x == 0 && blockIdx.x < nrows) stage(blockIdx.x, 0u);
+    for (uint32_t r = blockIdx.x; r < nrows; r += gridDim.x, k++) {
+        const uint32_t b = k & 1u;
+        // the other buffer was released at the end of the previous row
+        if (threadIdx.x == 0 && r + gridDim.x < nrows) stage(r + gridDim.x, b ^ 1u);
+        ok = mbar_wait(&bar[b], (k >> 1) & 1u, WAIT_LIMIT);
+        if (!__syncthreads_and(ok)) break;
+        const uint8_t* buf = rows_smem + b * RB;
+        const uint32_t y = r % ny, z = r / ny;
+        for (uint32_t x = threadIdx.x; x < nx; x += blockDim.x) {
+            const RowSrc<T> S{buf, nx, x, x + 1u == nx ? 0u : x + 1u, x == 0u ? nx - 1u : x - 1u, eb_off, fl_off};
+            sc_cell<19, FT, MHD, TRT, false, RowSrc<T>>(L, x + (y + z * ny) * nx, odd, S);
+        }
+        __syncthreads();  // buffer b is free
+    }
+    if (!ok && threadIdx.x == 0) {
+        // copies still in flight: this row's and possibly the next one's
+        const uint32_t b = k & 1u;
+        mbar_wait(&bar[b], (k >> 1) & 1u, WAIT_LIMIT);
+        if (blockIdx.x + (k + 1u) * gridDim.x < nrows) mbar_wait(&bar[b ^ 1u], ((k + 1u) >> 1) & 1u, WAIT_LIMIT);
+        atomicExch(err, 1u);
+    }
+}
+
+// the row kernel when the domain's rows can be copied as whole 16-byte-aligned
+// streams and two buffers fit in shared memory; false: use k_stream_collide
+template <int FT, bool MHD, bool TRT>
+bool launch_sc_rows(const DevLbm& L, uint32_t o, uint32_t* err, cudaStream_t s) {
+    if (L.nx % 16u || 2u * row_bytes<FT, MHD>(L.nx) > 200u * 1024u) return false;
+    const uint32_t smem = 2u * row_bytes<FT, MHD>(L.nx);
+    const uint32_t threads = ((L.nx + ((L.nx + 255u) / 256u) - 1u) / ((L.nx + 255u) / 256u) + 31u) / 32u * 32u;
+    static int max_smem = -1, per_sm = 0;
+    static uint32_t for_smem = 0, for_threads = 0;
+    if (max_smem < (int)smem) {
+        if (cudaFuncSetAttribute(k_sc_rows<FT, MHD, TRT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
+            cudaSuccess)
+            return false;
+        max_smem = 200 * 1024;
+    }
+    if (for_smem != smem || for_threads != threads) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sc_rows<FT, MHD, TRT>, (int)threads, smem) !=
+                cudaSuccess || per_sm < 1)
+            return false;
+        for_smem = smem;
+        for_threads = threads;
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    const uint32_t rows = L.ny * L.nz;
+    const uint32_t grid = std::min<uint32_t>(rows, (uint32_t)(per_sm * sms));
+    k_sc_rows<FT, MHD, TRT><<<grid, threads, smem, s>>>(L, o, err);
+    return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -486,7 +660,13 @@ __global__ void __launch_bounds__(256) k_update_fields(const DevLbm L, const uin
 
 // mode: 0 plain, 1 MAGNETO_HYDRO, 2 MAGNETO_HYDRO + SUBGRID_ECR
 template <int QV, int FT>
-void launch_sc(const DevLbm& L, int mode, bool trt, uint32_t o, unsigned g, cudaStream_t s) {
+void launch_sc(const DevLbm& L, int mode, bool trt, uint32_t o, unsigned g, uint32_t* err, cudaStream_t s) {
+    if constexpr (QV == 19) {
+        if (mode == 1 && (trt ? launch_sc_rows<FT, true, true>(L, o, err, s) : launch_sc_rows<FT, true, false>(L, o, err, s)))
+            return;
+        if (mode == 0 && (trt ? launch_sc_rows<FT, false, true>(L, o, err, s) : launch_sc_rows<FT, false, false>(L, o, err, s)))
+            return;
+    }
     if (mode == 2) {
         if (trt) k_stream_collide<QV, FT, true, true, true><<<g, 256, 0, s>>>(L, o);
         else k_stream_collide<QV, FT, true, false, true><<<g, 256, 0, s>>>(L, o);
@@ -506,12 +686,13 @@ void launch_init(const DevLbm& L, int mode, unsigned g, cudaStream_t s) {
 }
 
 #define ION_DEFINE_LBM_DISPATCH(QV, NAME)                                                                     \
-    void NAME##_stream_collide(const DevLbm& L, int ft, int mode, bool trt, uint64_t t, cudaStream_t s) {      \
+    void NAME##_stream_collide(const DevLbm& L, int ft, int mode, bool trt, uint64_t t, uint32_t* err,          \
+                               cudaStream_t s) {                                                               \
         const unsigned g = grid_for(L.n, 256);                                                                 \
         const uint32_t o = (uint32_t)(t & 1u);                                                                 \
-        if (ft == ION_FP32) launch_sc<QV, ION_FP32>(L, mode, trt, o, g, s);                                    \
-        else if (ft == ION_FP16S) launch_sc<QV, ION_FP16S>(L, mode, trt, o, g, s);                             \
-        else launch_sc<QV, ION_FP16C>(L, mode, trt, o, g, s);                                                  \
+        if (ft == ION_FP32) launch_sc<QV, ION_FP32>(L, mode, trt, o, g, err, s);                               \
+        else if (ft == ION_FP16S) launch_sc<QV, ION_FP16S>(L, mode, trt, o, g, err, s);                        \
+        else launch_sc<QV, ION_FP16C>(L, mode, trt, o, g, err, s);                                             \
     }                                                                                                          \
     void NAME##_initialize(const DevLbm& L, int ft, int mode, cudaStream_t s) {                                \
         const unsigned g = grid_for(L.n, 256);                                                                 \
