@@ -468,13 +468,14 @@ __global__ void __launch_bounds__(256, MHD ? 2 : 4) k_stream_collide(const DevLb
 
 // ---------------------------------------------------------------------------
 // D3Q19 stream_collide over x-rows staged in shared memory.  Each CTA walks rows
-// (y, z) = blockIdx.x, blockIdx.x + gridDim.x, ...; for the next row one thread
-// issues bulk asynchronous copies (cp.async.bulk, completion on the buffer's
+// (y, z) = blockIdx.x, blockIdx.x + gridDim.x, ...; a producer warp issues, for the
+// next row, bulk asynchronous copies (cp.async.bulk, completion on the buffer's "full"
 // mbarrier) of every stream the row's cells read -- per lattice the own-row slot of
 // DDF 0 and of each odd direction, and for each even direction the slot row of the
 // neighbour in the pair's direction (periodic in y and z; the x shift is applied
-// when reading) -- plus the E/B and flag rows, while the CTA computes the current
-// row from the other buffer.  All streams are contiguous rows, so the copies keep
+// when reading) -- plus the E/B and flag rows, while the compute warps work on the
+// current row from the other buffer and release it on its "empty" mbarrier (no
+// CTA-wide barrier per row, so warps with cheap rows do not wait for the others).  All streams are contiguous rows, so the copies keep
 // tens of KB per SM in flight without holding registers.  In Esoteric-Pull every
 // slot is read and written by the same cell within a step, so staging a row ahead
 // of its cells' stores is safe.  The arithmetic is sc_cell's (RowSrc only changes
@@ -491,72 +492,103 @@ __host__ __device__ inline uint32_t row_bytes(uint32_t nx) {
     return row_streams<FT, MHD>() * nx * (uint32_t)sizeof(T) + (MHD ? 6u * nx * 4u : 0u) + ((nx + 15u) & ~15u);
 }
 
+// waits for an mbarrier phase; gives up after WAIT_LIMIT polls (setting *fail) or as
+// soon as another warp has set *fail
+__device__ __forceinline__ bool mbar_wait_or_fail(uint64_t* bar, uint32_t parity, volatile uint32_t* fail) {
+    for (uint32_t i = 0; i < WAIT_LIMIT; i++) {
+        uint32_t done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+        if (done) return true;
+        if ((i & 255u) == 255u && *fail) return false;
+    }
+    *fail = 1u;
+    return false;
+}
+
+// blockDim.x = compute threads + 32: the last warp stages rows, the others compute
 template <int FT, bool MHD, bool TRT>
-__global__ void __launch_bounds__(256, 2) k_sc_rows(const DevLbm L, const uint32_t odd_t, uint32_t* err) {
+__global__ void __launch_bounds__(288, MHD ? 2 : 3) k_sc_rows(const DevLbm L, const uint32_t odd_t, uint32_t* err) {
     using V = VSet<19>;
     using T = typename Ddf<FT>::T;
     extern __shared__ __align__(128) uint8_t rows_smem[];
-    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ __align__(8) uint64_t full[2], empty[2];
+    __shared__ uint32_t fail_flag, issued;  // rows the producer has staged
+    volatile uint32_t* fail = &fail_flag;
     const bool odd = odd_t != 0u;
     const uint32_t nx = L.nx, ny = L.ny, nz = L.nz, nrows = ny * nz, N = L.n;
     const uint32_t rb = nx * (uint32_t)sizeof(T), RB = row_bytes<FT, MHD>(nx);
     const uint32_t eb_off = row_streams<FT, MHD>() * rb, fl_off = eb_off + (MHD ? 6u * nx * 4u : 0u);
+    const uint32_t nct = blockDim.x - 32u, ncw = nct / 32u;  // compute threads and warps
     if (threadIdx.x == 0) {
-        mbar_init(&bar[0], 1u);
-        mbar_init(&bar[1], 1u);
+        mbar_init(&full[0], 1u);
+        mbar_init(&full[1], 1u);
+        mbar_init(&empty[0], ncw);
+        mbar_init(&empty[1], ncw);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        fail_flag = 0u;
+        issued = 0u;
     }
     __syncthreads();
-    // copies of row r into buffer b (one thread)
-    auto stage = [&](uint32_t r, uint32_t b) {
-        uint8_t* dst = rows_smem + b * RB;
-        const uint32_t y = r % ny, z = r / ny;
-        const uint32_t own = (y + z * ny) * nx;
-        mbar_expect_tx(&bar[b], RB);
-        auto lattice = [&](const T* f, uint32_t base, int Q) {
-            bulk_g2s(dst + base * rb, f + own, rb, &bar[b]);
-            for (int i = 1; i < Q; i += 2) {
-                const int cy = Q == 7 ? (i == 3 ? 1 : 0) : V::c(i, 1), cz = Q == 7 ? (i == 5 ? 1 : 0) : V::c(i, 2);
-                const uint32_t yy = cy > 0 ? (y + 1u == ny ? 0u : y + 1u) : cy < 0 ? (y == 0u ? ny - 1u : y - 1u) : y;
-                const uint32_t zz = cz > 0 ? (z + 1u == nz ? 0u : z + 1u) : cz < 0 ? (z == 0u ? nz - 1u : z - 1u) : z;
-                const uint32_t s_own = odd ? (uint32_t)i : (uint32_t)i + 1u, s_nbr = odd ? (uint32_t)i + 1u : (uint32_t)i;
-                bulk_g2s(dst + (base + i) * rb, f + (size_t)s_own * N + own, rb, &bar[b]);
-                bulk_g2s(dst + (base + i + 1) * rb, f + (size_t)s_nbr * N + (yy + zz * ny) * nx, rb, &bar[b]);
-            }
-        };
-        lattice((const T*)L.fi, row_stream_base(LAT_FI), 19);
-        if constexpr (MHD) {
-            lattice((const T*)L.ei, row_stream_base(LAT_EI), 19);
-            lattice((const T*)L.fqi, row_stream_base(LAT_FQI), 7);
-            for (uint32_t c = 0; c < 3; c++) {
-                bulk_g2s(dst + eb_off + c * nx * 4u, L.b_dyn + (size_t)c * N + own, nx * 4u, &bar[b]);
-                bulk_g2s(dst + eb_off + (3u + c) * nx * 4u, L.e_dyn + (size_t)c * N + own, nx * 4u, &bar[b]);
+    const uint32_t my_rows = blockIdx.x < nrows ? (nrows - 1u - blockIdx.x) / gridDim.x + 1u : 0u;
+    if (threadIdx.x >= nct) {
+        // producer: row k of this CTA into buffer k & 1, once the compute warps released it
+        if (threadIdx.x == nct) {
+            for (uint32_t k = 0; k < my_rows; k++) {
+                const uint32_t b = k & 1u, r = blockIdx.x + k * gridDim.x;
+                if (k >= 2 && !mbar_wait_or_fail(&empty[b], ((k - 2) >> 1) & 1u, fail)) break;
+                if (*fail) break;
+                uint8_t* dst = rows_smem + b * RB;
+                const uint32_t y = r % ny, z = r / ny, own = (y + z * ny) * nx;
+                mbar_expect_tx(&full[b], RB);
+                auto lattice = [&](const T* f, uint32_t base, int Q) {
+                    bulk_g2s(dst + base * rb, f + own, rb, &full[b]);
+                    for (int i = 1; i < Q; i += 2) {
+                        const int cy = Q == 7 ? (i == 3 ? 1 : 0) : V::c(i, 1), cz = Q == 7 ? (i == 5 ? 1 : 0) : V::c(i, 2);
+                        const uint32_t yy = cy > 0 ? (y + 1u == ny ? 0u : y + 1u) : cy < 0 ? (y == 0u ? ny - 1u : y - 1u) : y;
+                        const uint32_t zz = cz > 0 ? (z + 1u == nz ? 0u : z + 1u) : cz < 0 ? (z == 0u ? nz - 1u : z - 1u) : z;
+                        const uint32_t s_own = odd ? (uint32_t)i : (uint32_t)i + 1u, s_nbr = odd ? (uint32_t)i + 1u : (uint32_t)i;
+                        bulk_g2s(dst + (base + i) * rb, f + (size_t)s_own * N + own, rb, &full[b]);
+                        bulk_g2s(dst + (base + i + 1) * rb, f + (size_t)s_nbr * N + (yy + zz * ny) * nx, rb, &full[b]);
+                    }
+                };
+                lattice((const T*)L.fi, row_stream_base(LAT_FI), 19);
+                if constexpr (MHD) {
+                    lattice((const T*)L.ei, row_stream_base(LAT_EI), 19);
+                    lattice((const T*)L.fqi, row_stream_base(LAT_FQI), 7);
+                    for (uint32_t c = 0; c < 3; c++) {
+                        bulk_g2s(dst + eb_off + c * nx * 4u, L.b_dyn + (size_t)c * N + own, nx * 4u, &full[b]);
+                        bulk_g2s(dst + eb_off + (3u + c) * nx * 4u, L.e_dyn + (size_t)c * N + own, nx * 4u, &full[b]);
+                    }
+                }
+                bulk_g2s(dst + fl_off, L.flags + own, (nx + 15u) & ~15u, &full[b]);
+                issued = k + 1u;
             }
         }
-        bulk_g2s(dst + fl_off, L.flags + own, (nx + 15u) & ~15u, &bar[b]);
-    };
-    uint32_t k = 0;
-    bool ok = true;
-    if (threadIdx.x == 0 && blockIdx.x < nrows) stage(blockIdx.x, 0u);
-    for (uint32_t r = blockIdx.x; r < nrows; r += gridDim.x, k++) {
-        const uint32_t b = k & 1u;
-        // the other buffer was released at the end of the previous row
-        if (threadIdx.x == 0 && r + gridDim.x < nrows) stage(r + gridDim.x, b ^ 1u);
-        ok = mbar_wait(&bar[b], (k >> 1) & 1u, WAIT_LIMIT);
-        if (!__syncthreads_and(ok)) break;
-        const uint8_t* buf = rows_smem + b * RB;
-        const uint32_t y = r % ny, z = r / ny;
-        for (uint32_t x = threadIdx.x; x < nx; x += blockDim.x) {
-            const RowSrc<T> S{buf, nx, x, x + 1u == nx ? 0u : x + 1u, x == 0u ? nx - 1u : x - 1u, eb_off, fl_off};
-            sc_cell<19, FT, MHD, TRT, false, RowSrc<T>>(L, x + (y + z * ny) * nx, odd, S);
+        __syncwarp();
+    } else {
+        const uint32_t lane = threadIdx.x & 31u;
+        for (uint32_t k = 0; k < my_rows; k++) {
+            const uint32_t b = k & 1u, r = blockIdx.x + k * gridDim.x;
+            const bool go = mbar_wait_or_fail(&full[b], (k >> 1) & 1u, fail) && *fail == 0u;
+            if (go) {
+                const uint8_t* buf = rows_smem + b * RB;
+                const uint32_t y = r % ny, z = r / ny;
+                for (uint32_t x = threadIdx.x; x < nx; x += nct) {
+                    const RowSrc<T> S{buf, nx, x, x + 1u == nx ? 0u : x + 1u, x == 0u ? nx - 1u : x - 1u, eb_off, fl_off};
+                    sc_cell<19, FT, MHD, TRT, false, RowSrc<T>>(L, x + (y + z * ny) * nx, odd, S);
+                }
+            }
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&empty[b])) : "memory");
         }
-        __syncthreads();  // buffer b is free
     }
-    if (!ok && threadIdx.x == 0) {
-        // copies still in flight: this row's and possibly the next one's
-        const uint32_t b = k & 1u;
-        mbar_wait(&bar[b], (k >> 1) & 1u, WAIT_LIMIT);
-        if (blockIdx.x + (k + 1u) * gridDim.x < nrows) mbar_wait(&bar[b ^ 1u], ((k + 1u) >> 1) & 1u, WAIT_LIMIT);
+    __syncthreads();
+    if (threadIdx.x == 0 && *fail) {
+        // copies that may still be in flight: the last two rows the producer staged
+        const uint32_t n_issued = issued;
+        for (uint32_t k = n_issued > 2u ? n_issued - 2u : 0u; k < n_issued; k++)
+            mbar_wait(&full[k & 1u], (k >> 1) & 1u, WAIT_LIMIT);
         atomicExch(err, 1u);
     }
 }
@@ -567,7 +599,8 @@ template <int FT, bool MHD, bool TRT>
 bool launch_sc_rows(const DevLbm& L, uint32_t o, uint32_t* err, cudaStream_t s) {
     if (L.nx % 16u || 2u * row_bytes<FT, MHD>(L.nx) > 200u * 1024u) return false;
     const uint32_t smem = 2u * row_bytes<FT, MHD>(L.nx);
-    const uint32_t threads = ((L.nx + ((L.nx + 255u) / 256u) - 1u) / ((L.nx + 255u) / 256u) + 31u) / 32u * 32u;
+    // compute threads (x-cells per thread = ceil(nx / 256)) plus the producer warp
+    const uint32_t threads = ((L.nx + ((L.nx + 255u) / 256u) - 1u) / ((L.nx + 255u) / 256u) + 31u) / 32u * 32u + 32u;
     static int max_smem = -1, per_sm = 0;
     static uint32_t for_smem = 0, for_threads = 0;
     if (max_smem < (int)smem) {
