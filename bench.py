@@ -60,8 +60,14 @@ FLOP_PER_INTERACTION = 34  # one source's E and B: 34 FLOP + 1 sqrt (sim_kernels
 # the summaries with the commands that produced them are in profiles/
 # (rings384: the 192^3 capture of the same kernel scaled by the cell count, 8x; its traffic is
 # proportional to the cells)
-NCU_TRAFFIC = {("tgv256", "k_stream_collide"): 2.507149e9, ("mhd128", "k_stream_collide"): 0.795728e9,
-               ("mhd128", "k_update_e_b_fast"): 63.567e6, ("rings384", "k_stream_collide"): 12.8329e9}
+NCU_TRAFFIC = {("mhd128", "k_update_e_b_fast"): 63.567e6}
+
+
+def stencil_kernel(cfg: dict) -> str:
+    """The stream_collide kernel the library launches for a domain: the row-staged
+    D3Q19 kernel when rows are whole 16-byte streams (and not SUBGRID_ECR)."""
+    rows = cfg.get("velocity_set", 2) == 2 and not cfg.get("ext_subgrid_ecr") and cfg["n_x"] % 16 == 0
+    return "k_sc_rows" if rows else "k_stream_collide"
 
 
 def parse():
@@ -481,9 +487,10 @@ def main():
         bins_ms, _ = lbm.kernel_time(2)
         sc_avg = sc_ms / max(sc_n, 1)
         gbs = cells * bpl / (sc_avg * 1e-3) / 1e9
-        tr = NCU_TRAFFIC.get((a.workload, "k_stream_collide"))
+        sk = stencil_kernel(cases[0]["config"])
+        tr = NCU_TRAFFIC.get((a.workload, sk))
         roof_stencil = {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
-                        "traffic": tr, "kernel": "k_stream_collide", "bytes_per_lup": bpl,
+                        "traffic": tr, "kernel": sk, "bytes_per_lup": bpl,
                         "bytes_per_launch": cells * bpl, "avg_launch_ms": sc_avg, "peak_source": hbm_src}
         share = {"stream_collide_ms": sc_ms}
         roofline = roof_stencil

@@ -468,20 +468,21 @@ __global__ void __launch_bounds__(256, MHD ? 2 : 4) k_stream_collide(const DevLb
 
 // ---------------------------------------------------------------------------
 // D3Q19 stream_collide over x-rows staged in shared memory.  Each CTA walks rows
-// (y, z) = blockIdx.x, blockIdx.x + gridDim.x, ...; a producer warp issues, for the
-// next row, bulk asynchronous copies (cp.async.bulk, completion on the buffer's "full"
-// mbarrier) of every stream the row's cells read -- per lattice the own-row slot of
-// DDF 0 and of each odd direction, and for each even direction the slot row of the
-// neighbour in the pair's direction (periodic in y and z; the x shift is applied
-// when reading) -- plus the E/B and flag rows, while the compute warps work on the
-// current row from the other buffer and release it on its "empty" mbarrier (no
-// CTA-wide barrier per row, so warps with cheap rows do not wait for the others).  All streams are contiguous rows, so the copies keep
-// tens of KB per SM in flight without holding registers.  In Esoteric-Pull every
-// slot is read and written by the same cell within a step, so staging a row ahead
-// of its cells' stores is safe.  The arithmetic is sc_cell's (RowSrc only changes
-// where values are read); stores go to global memory as before.  A copy that does
-// not land within the wait limit sets *err and the CTA stops after waiting (bounded)
-// for its copies in flight.
+// (y, z) = blockIdx.x, blockIdx.x + gridDim.x, ...; for the next row it issues bulk
+// asynchronous copies (cp.async.bulk, completion on the buffer's mbarrier) of every
+// stream the row's cells read -- per lattice the own-row slot of DDF 0 and of each
+// odd direction, and for each even direction the slot row of the neighbour in the
+// pair's direction (periodic in y and z; the x shift is applied when reading) --
+// plus the E/B and flag rows, while the row before is computed from the other
+// buffer.  All streams are contiguous rows, so the copies keep tens of KB per SM in
+// flight without holding registers.  In Esoteric-Pull every slot is read and
+// written by the same cell within a step, so staging a row ahead of its cells'
+// stores is safe.  The arithmetic is sc_cell's (RowSrc only changes where values
+// are read); stores go to global memory as before.  Two forms: k_sc_rows_ws (rows
+// of up to 256 cells: a producer warp and "full"/"empty" mbarriers, no CTA-wide
+// barrier per row) and k_sc_rows (longer rows: thread 0 stages, a CTA barrier
+// releases the buffer).  A copy that does not land within the wait limit sets
+// *err and the CTA stops after waiting (bounded) for its copies in flight.
 // ---------------------------------------------------------------------------
 template <int FT, bool MHD>
 __host__ __device__ constexpr uint32_t row_streams() { return MHD ? 45u : 19u; }
@@ -490,6 +491,80 @@ template <int FT, bool MHD>
 __host__ __device__ inline uint32_t row_bytes(uint32_t nx) {
     using T = typename Ddf<FT>::T;
     return row_streams<FT, MHD>() * nx * (uint32_t)sizeof(T) + (MHD ? 6u * nx * 4u : 0u) + ((nx + 15u) & ~15u);
+}
+
+// Rows longer than 256 cells: CTAs of at most 256 threads, each thread two cells of
+// the row; thread 0 stages the next row at the start of each row and a CTA barrier
+// releases a buffer (measured faster than the producer-warp form at 384 cells, where
+// two cells per thread want the registers the extra warp would take).
+template <int FT, bool MHD, bool TRT>
+__global__ void __launch_bounds__(256, 2) k_sc_rows(const DevLbm L, const uint32_t odd_t, uint32_t* err) {
+    using V = VSet<19>;
+    using T = typename Ddf<FT>::T;
+    extern __shared__ __align__(128) uint8_t rows_smem[];
+    __shared__ __align__(8) uint64_t bar[2];
+    const bool odd = odd_t != 0u;
+    const uint32_t nx = L.nx, ny = L.ny, nz = L.nz, nrows = ny * nz, N = L.n;
+    const uint32_t rb = nx * (uint32_t)sizeof(T), RB = row_bytes<FT, MHD>(nx);
+    const uint32_t eb_off = row_streams<FT, MHD>() * rb, fl_off = eb_off + (MHD ? 6u * nx * 4u : 0u);
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1u);
+        mbar_init(&bar[1], 1u);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    // copies of row r into buffer b (one thread)
+    auto stage = [&](uint32_t r, uint32_t b) {
+        uint8_t* dst = rows_smem + b * RB;
+        const uint32_t y = r % ny, z = r / ny;
+        const uint32_t own = (y + z * ny) * nx;
+        mbar_expect_tx(&bar[b], RB);
+        auto lattice = [&](const T* f, uint32_t base, int Q) {
+            bulk_g2s(dst + base * rb, f + own, rb, &bar[b]);
+            for (int i = 1; i < Q; i += 2) {
+                const int cy = Q == 7 ? (i == 3 ? 1 : 0) : V::c(i, 1), cz = Q == 7 ? (i == 5 ? 1 : 0) : V::c(i, 2);
+                const uint32_t yy = cy > 0 ? (y + 1u == ny ? 0u : y + 1u) : cy < 0 ? (y == 0u ? ny - 1u : y - 1u) : y;
+                const uint32_t zz = cz > 0 ? (z + 1u == nz ? 0u : z + 1u) : cz < 0 ? (z == 0u ? nz - 1u : z - 1u) : z;
+                const uint32_t s_own = odd ? (uint32_t)i : (uint32_t)i + 1u, s_nbr = odd ? (uint32_t)i + 1u : (uint32_t)i;
+                bulk_g2s(dst + (base + i) * rb, f + (size_t)s_own * N + own, rb, &bar[b]);
+                bulk_g2s(dst + (base + i + 1) * rb, f + (size_t)s_nbr * N + (yy + zz * ny) * nx, rb, &bar[b]);
+            }
+        };
+        lattice((const T*)L.fi, row_stream_base(LAT_FI), 19);
+        if constexpr (MHD) {
+            lattice((const T*)L.ei, row_stream_base(LAT_EI), 19);
+            lattice((const T*)L.fqi, row_stream_base(LAT_FQI), 7);
+            for (uint32_t c = 0; c < 3; c++) {
+                bulk_g2s(dst + eb_off + c * nx * 4u, L.b_dyn + (size_t)c * N + own, nx * 4u, &bar[b]);
+                bulk_g2s(dst + eb_off + (3u + c) * nx * 4u, L.e_dyn + (size_t)c * N + own, nx * 4u, &bar[b]);
+            }
+        }
+        bulk_g2s(dst + fl_off, L.flags + own, (nx + 15u) & ~15u, &bar[b]);
+    };
+    uint32_t k = 0;
+    bool ok = true;
+    if (threadIdx.x == 0 && blockIdx.x < nrows) stage(blockIdx.x, 0u);
+    for (uint32_t r = blockIdx.x; r < nrows; r += gridDim.x, k++) {
+        const uint32_t b = k & 1u;
+        // the other buffer was released at the end of the previous row
+        if (threadIdx.x == 0 && r + gridDim.x < nrows) stage(r + gridDim.x, b ^ 1u);
+        ok = mbar_wait(&bar[b], (k >> 1) & 1u, WAIT_LIMIT);
+        if (!__syncthreads_and(ok)) break;
+        const uint8_t* buf = rows_smem + b * RB;
+        const uint32_t y = r % ny, z = r / ny;
+        for (uint32_t x = threadIdx.x; x < nx; x += blockDim.x) {
+            const RowSrc<T> S{buf, nx, x, x + 1u == nx ? 0u : x + 1u, x == 0u ? nx - 1u : x - 1u, eb_off, fl_off};
+            sc_cell<19, FT, MHD, TRT, false, RowSrc<T>>(L, x + (y + z * ny) * nx, odd, S);
+        }
+        __syncthreads();  // buffer b is free
+    }
+    if (!ok && threadIdx.x == 0) {
+        // copies still in flight: this row's and possibly the next one's
+        const uint32_t b = k & 1u;
+        mbar_wait(&bar[b], (k >> 1) & 1u, WAIT_LIMIT);
+        if (blockIdx.x + (k + 1u) * gridDim.x < nrows) mbar_wait(&bar[b ^ 1u], ((k + 1u) >> 1) & 1u, WAIT_LIMIT);
+        atomicExch(err, 1u);
+    }
 }
 
 // waits for an mbarrier phase; gives up after WAIT_LIMIT polls (setting *fail) or as
@@ -506,9 +581,10 @@ __device__ __forceinline__ bool mbar_wait_or_fail(uint64_t* bar, uint32_t parity
     return false;
 }
 
-// blockDim.x = compute threads + 32: the last warp stages rows, the others compute
+// Rows of up to 256 cells: blockDim.x = compute threads + 32; the last warp stages rows,
+// the others compute (one cell per thread and row)
 template <int FT, bool MHD, bool TRT>
-__global__ void __launch_bounds__(288, MHD ? 2 : 3) k_sc_rows(const DevLbm L, const uint32_t odd_t, uint32_t* err) {
+__global__ void __launch_bounds__(288, MHD ? 2 : 3) k_sc_rows_ws(const DevLbm L, const uint32_t odd_t, uint32_t* err) {
     using V = VSet<19>;
     using T = typename Ddf<FT>::T;
     extern __shared__ __align__(128) uint8_t rows_smem[];
@@ -593,34 +669,36 @@ __global__ void __launch_bounds__(288, MHD ? 2 : 3) k_sc_rows(const DevLbm L, co
     }
 }
 
-// the row kernel when the domain's rows can be copied as whole 16-byte-aligned
+// the row kernels when the domain's rows can be copied as whole 16-byte-aligned
 // streams and two buffers fit in shared memory; false: use k_stream_collide
 template <int FT, bool MHD, bool TRT>
 bool launch_sc_rows(const DevLbm& L, uint32_t o, uint32_t* err, cudaStream_t s) {
     if (L.nx % 16u || 2u * row_bytes<FT, MHD>(L.nx) > 200u * 1024u) return false;
     const uint32_t smem = 2u * row_bytes<FT, MHD>(L.nx);
-    // compute threads (x-cells per thread = ceil(nx / 256)) plus the producer warp
-    const uint32_t threads = ((L.nx + ((L.nx + 255u) / 256u) - 1u) / ((L.nx + 255u) / 256u) + 31u) / 32u * 32u + 32u;
-    static int max_smem = -1, per_sm = 0;
-    static uint32_t for_smem = 0, for_threads = 0;
-    if (max_smem < (int)smem) {
-        if (cudaFuncSetAttribute(k_sc_rows<FT, MHD, TRT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
-            cudaSuccess)
-            return false;
-        max_smem = 200 * 1024;
+    const bool ws = L.nx <= 256u;  // producer warp + one cell per thread and row
+    const uint32_t threads =
+        ws ? (L.nx + 31u) / 32u * 32u + 32u : ((L.nx + ((L.nx + 255u) / 256u) - 1u) / ((L.nx + 255u) / 256u) + 31u) / 32u * 32u;
+    auto kern = ws ? k_sc_rows_ws<FT, MHD, TRT> : k_sc_rows<FT, MHD, TRT>;
+    static bool attr[2] = {false, false};
+    static int per_sm[2] = {0, 0};
+    static uint32_t for_smem[2] = {0, 0}, for_threads[2] = {0, 0};
+    const int v = ws ? 1 : 0;
+    if (!attr[v]) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess) return false;
+        attr[v] = true;
     }
-    if (for_smem != smem || for_threads != threads) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sc_rows<FT, MHD, TRT>, (int)threads, smem) !=
-                cudaSuccess || per_sm < 1)
+    if (for_smem[v] != smem || for_threads[v] != threads) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[v], kern, (int)threads, smem) != cudaSuccess ||
+            per_sm[v] < 1)
             return false;
-        for_smem = smem;
-        for_threads = threads;
+        for_smem[v] = smem;
+        for_threads[v] = threads;
     }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
     const uint32_t rows = L.ny * L.nz;
-    const uint32_t grid = std::min<uint32_t>(rows, (uint32_t)(per_sm * sms));
-    k_sc_rows<FT, MHD, TRT><<<grid, threads, smem, s>>>(L, o, err);
+    const uint32_t grid = std::min<uint32_t>(rows, (uint32_t)(per_sm[v] * sms));
+    kern<<<grid, threads, smem, s>>>(L, o, err);
     return true;
 }
 

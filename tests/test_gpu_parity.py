@@ -211,3 +211,14 @@ def test_subgrid_ecr_bitwise(ft, rt):
     g.finish_queues(60000)
     o.run(2)
     assert U.compare_bitwise(g, o, names) == {n: 0 for n in names}
+
+
+@pytest.mark.parametrize("ft", [2, 0], ids=["FP32", "FP16S"])
+def test_long_rows_bitwise(ft):
+    """Rows longer than 256 cells take the other row-staged stream_collide form:
+    an elongated MHD box (272 x 16 x 16) bit-identical to the oracle after 2 steps."""
+    case = W.mhd_box(shape=(272, 16, 16), depth=2, magnet_r=5.0, magnet_t=3.0, float_type=ft)
+    g = U.run_gpu(case, 2)
+    o = orc_run(case, 2)
+    diff = U.compare_bitwise(g, o, U.field_names(case))
+    assert all(v == 0 for v in diff.values()), diff
