@@ -58,16 +58,19 @@ sys.path.insert(0, str(ROOT))
 FLOP_PER_INTERACTION = 34  # one source's E and B: 34 FLOP + 1 sqrt (sim_kernels.cl:950-954)
 # kernel-time results of one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum per launch);
 # the summaries with the commands that produced them are in profiles/
-# (rings384: the 192^3 capture of the same kernel scaled by the cell count, 8x; its traffic is
-# proportional to the cells)
-NCU_TRAFFIC = {("mhd128", "k_update_e_b_fast"): 63.567e6}
+# (rings384: the 192^3 capture of the row-staged stencil scaled by the cell count, 8x; both
+# row forms copy the same streams per cell, so the traffic is proportional to the cells)
+NCU_TRAFFIC = {("tgv256", "k_sc_rows_ws"): 2.506631e9, ("mhd128", "k_sc_rows_ws"): 0.807230e9,
+               ("mhd128", "k_update_e_b_fast"): 63.567e6, ("rings384", "k_sc_rows"): 8 * 1.614150e9}
 
 
 def stencil_kernel(cfg: dict) -> str:
     """The stream_collide kernel the library launches for a domain: the row-staged
     D3Q19 kernel when rows are whole 16-byte streams (and not SUBGRID_ECR)."""
     rows = cfg.get("velocity_set", 2) == 2 and not cfg.get("ext_subgrid_ecr") and cfg["n_x"] % 16 == 0
-    return "k_sc_rows" if rows else "k_stream_collide"
+    if not rows:
+        return "k_stream_collide"
+    return "k_sc_rows_ws" if cfg["n_x"] <= 256 else "k_sc_rows"
 
 
 def parse():
