@@ -368,10 +368,17 @@ __device__ __forceinline__ void near_field(const DevLbm& L, uint32_t n, uint32_t
             }
 }
 
+// One past the last source bin summed.  Bins [8^D, n_lod_own) are cleared every step
+// (clear_qu_lod, sim_kernels.cl:995-1003), so their terms are exact zeros: FAST stops at
+// 8^D (14% fewer terms at every depth); BITWISE adds them as the reference does (a zero
+// term can turn a -0.0 sum into +0.0).
+template <bool FAST>
+__device__ __forceinline__ uint32_t src_last(const DevLbm& L) { return FAST ? min(L.n_lod_own, L.n_bins) : L.n_lod_own; }
+
 // Issues the bulk copies of source chunk c into buffer c & 1 (one thread).
 template <class SM>
-__device__ __forceinline__ void eb_issue(const DevLbm& L, SM& sm, uint32_t c) {
-    const uint32_t first = L.first_src, last = L.n_lod_own;
+__device__ __forceinline__ void eb_issue(const DevLbm& L, SM& sm, uint32_t c, uint32_t last) {
+    const uint32_t first = L.first_src;
     const uint32_t base = first + c * SRC_CHUNK;
     const uint32_t cnt = min(SRC_CHUNK, last - base);
     const uint32_t buf = c & 1u;
@@ -439,14 +446,14 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t brick, c
     }
 
     // depth-D LOD bins [first_src, n_lod_own) except the cell's own (sim_kernels.cl:940-955)
-    const uint32_t first = L.first_src, last = L.n_lod_own;
+    const uint32_t first = L.first_src, last = src_last<FAST>(L);
     const uint32_t nchunks = (last - first + SRC_CHUNK - 1u) / SRC_CHUNK;
-    if (threadIdx.x == 0 && nchunks > 0) eb_issue(L, sm, 0);
+    if (threadIdx.x == 0 && nchunks > 0) eb_issue(L, sm, 0, last);
     bool ok = true;
     uint32_t c = 0;
     for (; c < nchunks; c++) {
         const uint32_t buf = c & 1u;
-        if (threadIdx.x == 0 && c + 1 < nchunks) eb_issue(L, sm, c + 1);
+        if (threadIdx.x == 0 && c + 1 < nchunks) eb_issue(L, sm, c + 1, last);
         const bool landed = mbar_wait(&sm.bar[buf], uses[buf] & 1u, WAIT_LIMIT);
         ok = __syncthreads_and(landed) != 0;  // block-uniform
         if (!ok) break;

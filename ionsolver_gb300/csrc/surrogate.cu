@@ -772,7 +772,8 @@ __global__ void __launch_bounds__(128) k_sample_check(const DevLbm L, uint32_t c
     const uint32_t own = x / L.bsx + (y / L.bsy + z / L.bsz * L.nd) * L.nd;
     float e[3] = {0, 0, 0}, b[3] = {0, 0, 0};
     const float4* qu = (const float4*)L.qu_lod;
-    for (uint32_t d = L.first_src + lane; d < L.n_lod_own; d += 32u) {
+    const uint32_t last = src_last<true>(L);  // bins from 8^D on are always zero
+    for (uint32_t d = L.first_src + lane; d < last; d += 32u) {
         if (d == own) continue;
         const float4 p = L.lod_pos[d], v = qu[d];
         add_src<true>((float)x - p.x, (float)y - p.y, (float)z - p.z, make_float4(v.x, v.x * v.y, v.x * v.z, v.x * v.w),
