@@ -595,7 +595,7 @@ __device__ __forceinline__ void quad_weights(float t, float* w) {  // Lagrange w
 __device__ __forceinline__ void surrogate_tile(const DevLbm& L, SurSmem& sm, uint32_t bin, int bx, int by, int bz,
                                                uint32_t tile, uint32_t cells, const Magic& mx, const Magic& mxy);
 
-__global__ void __launch_bounds__(SC_THREADS, 3) k_surrogate_cells(const DevLbm L, const float* Y, const float* G,
+__global__ void __launch_bounds__(SC_THREADS, 2) k_surrogate_cells(const DevLbm L, const float* Y, const float* G,
                                                                 const float* scales, float yE, float yB) {
     extern __shared__ __align__(16) uint8_t sur_smem[];  // sizeof(SurSmem), above the 48 KB of static shared memory
     SurSmem& sm = *reinterpret_cast<SurSmem*>(sur_smem);
@@ -699,11 +699,14 @@ __device__ __forceinline__ void surrogate_tile(const DevLbm& L, SurSmem& sm, uin
         far_zero(fs[j]);
     }
     const uint32_t cnt = sm.count;
+    // the next source's values are read from shared memory while this one is summed
+    FastSrc S = sm.src[0];
 #pragma unroll 1
     for (uint32_t s = 0; s < cnt; s++) {
-        const FastSrc S = sm.src[s];
+        const FastSrc Sn = sm.src[s + 1u < cnt ? s + 1u : s];
 #pragma unroll
         for (uint32_t j = 0; j < SC_CPT / 2; j++) far_fast2(cp[j], cc[j], S, fs[j]);
+        S = Sn;
     }
     asm volatile("cp.async.commit_group;\n cp.async.wait_group 0;" ::: "memory");
 #pragma unroll
