@@ -80,8 +80,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="mhd128",
-                   choices=["mhd128", "mhd256", "mhd64", "batch96", "rings384", "rings192", "tgv64", "tgv256",
-                            "tgv384"])
+                   choices=["mhd128", "mhd256", "mhd64", "batch96", "rings384", "rings192", "rings192d3", "tgv64",
+                            "tgv256", "tgv384"])
     p.add_argument("--field-mode", default=None, choices=["bitwise", "fast", "surrogate"],
                    help="default: surrogate for rings384, fast otherwise")
     p.add_argument("--float-type", default=None, choices=["FP32", "FP16S", "FP16C"],
@@ -111,8 +111,9 @@ def make_cases(a) -> list[dict]:
     w = a.workload
     if w == "batch96":
         return W.batch_domains(96, float_type=ft, field_mode=fm)
-    if w.startswith("rings"):  # rings192: the same box at half the size (profiling case)
-        return [W.mhd_box(n=int(w[5:]), float_type=ft, depth=4, field_mode=fm, rings=True)]
+    if w.startswith("rings"):  # rings192: the same box at half the size; rings192d3: LOD depth 3, i.e. the
+        n, _, d = w[5:].partition("d")  # 24^3-cell bins of rings384 (profiling cases)
+        return [W.mhd_box(n=int(n), float_type=ft, depth=int(d or 4), field_mode=fm, rings=True)]
     n = int(w[3:])
     if w.startswith("mhd"):
         return [W.mhd_box(n=n, float_type=ft, field_mode=fm, magnet_r=16.0 * n / 128, magnet_t=8.0 * n / 128)]
