@@ -10,6 +10,7 @@
 // separate pass (field_kernels.cu) sums every bin in ascending cell order.
 #pragma once
 #include <algorithm>
+#include <mutex>
 
 #include "ion_device.cuh"
 #include "ion_launch.h"
@@ -679,25 +680,34 @@ bool launch_sc_rows(const DevLbm& L, uint32_t o, uint32_t* err, cudaStream_t s) 
     const uint32_t threads =
         ws ? (L.nx + 31u) / 32u * 32u + 32u : ((L.nx + ((L.nx + 255u) / 256u) - 1u) / ((L.nx + 255u) / 256u) + 31u) / 32u * 32u;
     auto kern = ws ? k_sc_rows_ws<FT, MHD, TRT> : k_sc_rows<FT, MHD, TRT>;
+    // the shared-memory opt-in and the occupancy of the last shape, per instantiation
+    // (handles may step on several host threads)
+    static std::mutex mu;
     static bool attr[2] = {false, false};
-    static int per_sm[2] = {0, 0};
+    static int per_sm_of[2] = {0, 0};
     static uint32_t for_smem[2] = {0, 0}, for_threads[2] = {0, 0};
     const int v = ws ? 1 : 0;
-    if (!attr[v]) {
-        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess) return false;
-        attr[v] = true;
-    }
-    if (for_smem[v] != smem || for_threads[v] != threads) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[v], kern, (int)threads, smem) != cudaSuccess ||
-            per_sm[v] < 1)
-            return false;
-        for_smem[v] = smem;
-        for_threads[v] = threads;
+    int per_sm = 0;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!attr[v]) {
+            if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess)
+                return false;
+            attr[v] = true;
+        }
+        if (for_smem[v] != smem || for_threads[v] != threads) {
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_of[v], kern, (int)threads, smem) != cudaSuccess ||
+                per_sm_of[v] < 1)
+                return false;
+            for_smem[v] = smem;
+            for_threads[v] = threads;
+        }
+        per_sm = per_sm_of[v];
     }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
     const uint32_t rows = L.ny * L.nz;
-    const uint32_t grid = std::min<uint32_t>(rows, (uint32_t)(per_sm[v] * sms));
+    const uint32_t grid = std::min<uint32_t>(rows, (uint32_t)(per_sm * sms));
     kern<<<grid, threads, smem, s>>>(L, o, err);
     return true;
 }
