@@ -40,10 +40,12 @@ def test_other_velocity_sets_bitwise(vs, shape):
     assert U.compare_bitwise(g, o, ["fi", "rho", "u"]) == {"fi": 0, "rho": 0, "u": 0}
 
 
+@pytest.mark.parametrize("nx", [24, 32], ids=["global-loads", "row-staged"])
 @pytest.mark.parametrize("rt", [0, 1], ids=["SRT", "TRT"])
-def test_boundaries_and_forces_bitwise(rt):
-    """Solid cells, equilibrium (inflow/outflow) cells, volume force and force field."""
-    nx, ny, nz = 24, 20, 16
+def test_boundaries_and_forces_bitwise(rt, nx):
+    """Solid cells, equilibrium (inflow/outflow) cells, volume force and force field
+    (rows of 24 cells run the global-load stream_collide, rows of 32 the row-staged one)."""
+    ny, nz = 20, 16
     N = nx * ny * nz
     rng = np.random.default_rng(7)
     case = W.taylor_green(shape=(nx, ny, nz), amplitude=0.03, relaxation_time=rt)
@@ -213,12 +215,33 @@ def test_subgrid_ecr_bitwise(ft, rt):
     assert U.compare_bitwise(g, o, names) == {n: 0 for n in names}
 
 
-@pytest.mark.parametrize("ft", [2, 0], ids=["FP32", "FP16S"])
-def test_long_rows_bitwise(ft):
+@pytest.mark.parametrize("ft,rt", [(2, 0), (0, 0), (1, 1)], ids=["FP32-SRT", "FP16S-SRT", "FP16C-TRT"])
+def test_long_rows_bitwise(ft, rt):
     """Rows longer than 256 cells take the other row-staged stream_collide form:
     an elongated MHD box (272 x 16 x 16) bit-identical to the oracle after 2 steps."""
     case = W.mhd_box(shape=(272, 16, 16), depth=2, magnet_r=5.0, magnet_t=3.0, float_type=ft)
+    case["config"]["relaxation_time"] = rt
     g = U.run_gpu(case, 2)
     o = orc_run(case, 2)
+    diff = U.compare_bitwise(g, o, U.field_names(case))
+    assert all(v == 0 for v in diff.values()), diff
+
+
+@pytest.mark.parametrize("ft", [2, 0, 1], ids=["FP32", "FP16S", "FP16C"])
+def test_long_rows_plain_trt_bitwise(ft):
+    """The long-row form without MHD: a 288 x 8 x 8 Taylor-Green box, TRT, 20 steps."""
+    case = W.taylor_green(shape=(288, 8, 8), amplitude=0.05, float_type=ft, relaxation_time=1)
+    g = U.run_gpu(case, 20)
+    o = orc_run(case, 20)
+    assert U.compare_bitwise(g, o, ["fi", "rho", "u"]) == {"fi": 0, "rho": 0, "u": 0}
+
+
+@pytest.mark.parametrize("ft", [2, 0, 1], ids=["FP32", "FP16S", "FP16C"])
+def test_mhd_trt_bitwise(ft):
+    """MHD with TRT collision through the row-staged stream_collide (32^3, depth 4)."""
+    case = W.mhd_box(n=32, float_type=ft, depth=4, magnet_r=6.0, magnet_t=4.0, field_mode=0)
+    case["config"]["relaxation_time"] = 1
+    g = U.run_gpu(case, 8)
+    o = orc_run(case, 8)
     diff = U.compare_bitwise(g, o, U.field_names(case))
     assert all(v == 0 for v in diff.values()), diff
