@@ -114,25 +114,22 @@ __host__ __device__ __forceinline__ uint16_t fp16c_encode(float x) {
     const uint32_t xb = fbits(x);
     const uint32_t b = (((xb & 0x7FFFFFFFu) > 0x7F800000u) ? 0x7FFFFFFFu : xb) + 0x800u;
     const uint32_t e = (b & 0x7F800000u) >> 23, m = b & 0x007FFFFFu;
-    uint32_t out = (b & 0x80000000u) >> 16;
-    if (e > 112u) out |= (((e - 112u) << 11) & 0x7800u) | (m >> 12);
-    else if (e > 100u) out |= (((0x007FF800u + m) >> (124u - e)) + 1u) >> 1;
-    return (uint16_t)out;
+    // both candidates, then a select (no divergent branch when a warp mixes normal and
+    // subnormal results): normal for e > 112, subnormal (shift clamped into 12..23) for
+    // 100 < e <= 112, zero below
+    const uint32_t nrm = (((e - 112u) << 11) & 0x7800u) | (m >> 12);
+    const uint32_t es = e < 101u ? 101u : (e > 112u ? 112u : e);
+    const uint32_t sub = (((0x007FF800u + m) >> (124u - es)) + 1u) >> 1;
+    return (uint16_t)(((b & 0x80000000u) >> 16) | (e > 112u ? nrm : (e > 100u ? sub : 0u)));
 }
 __host__ __device__ __forceinline__ float fp16c_decode(uint16_t x) {
-    const uint32_t e = (x & 0x7800u) >> 11, m = (uint32_t)(x & 0x07FFu) << 12;
-    uint32_t out = (uint32_t)(x & 0x8000u) << 16;
-    if (e != 0u) {
-        out |= ((e + 112u) << 23) | m;
-    } else if (m != 0u) {
-#ifdef __CUDA_ARCH__
-        const uint32_t lead = 31u - (uint32_t)__clz(m);
-#else
-        const uint32_t lead = 31u - (uint32_t)__builtin_clz(m);
-#endif
-        out |= ((lead + 90u) << 23) | ((m << (23u - lead)) & 0x007FF000u);
-    }
-    return bitsf(out);
+    const uint32_t mag = x & 0x7FFFu, sign = (uint32_t)(x & 0x8000u) << 16;
+    // exponent field > 0: sign | (e + 112) << 23 | m << 12, one shift and one add;
+    // exponent field 0: m * 2^-25 exactly (m < 2^11), which is the normalised float the
+    // leading-zero count would build
+    const uint32_t nrm = (mag << 12) + (112u << 23);
+    const uint32_t sub = fbits((float)mag * 2.98023223876953125e-8f);
+    return bitsf(sign | (mag >= 0x0800u ? nrm : sub));
 }
 
 // shared memory, mbarriers and bulk asynchronous copies (cp.async.bulk, completion
