@@ -368,12 +368,15 @@ __device__ __forceinline__ void near_field(const DevLbm& L, uint32_t n, uint32_t
             }
 }
 
-// One past the last source bin summed.  Bins [8^D, n_lod_own) are cleared every step
-// (clear_qu_lod, sim_kernels.cl:995-1003), so their terms are exact zeros: FAST stops at
-// 8^D (14% fewer terms at every depth); BITWISE adds them as the reference does (a zero
-// term can turn a -0.0 sum into +0.0).
+// One past the last source bin summed.  The reference reads bins [n_lod_own - 8^D,
+// n_lod_own), but its bin sums only write indices below 8^D and clear_qu_lod
+// (sim_kernels.cl:995-1003) zeroes the rest every step, so the trailing n_lod_own - 8^D
+// terms are q = 0 times a finite factor (those bins lie outside the box): +-0.  Adding
+// +-0 changes no sum here -- a sum starts at +0 and, under round-to-nearest, can only
+// become +0 again by cancellation, never -0 -- so both modes stop at 8^D and BITWISE
+// stays bit-identical (14% fewer terms at every depth).
 template <bool FAST>
-__device__ __forceinline__ uint32_t src_last(const DevLbm& L) { return FAST ? min(L.n_lod_own, L.n_bins) : L.n_lod_own; }
+__device__ __forceinline__ uint32_t src_last(const DevLbm& L) { return min(L.n_lod_own, L.n_bins); }
 
 // Issues the bulk copies of source chunk c into buffer c & 1 (one thread).
 template <class SM>
