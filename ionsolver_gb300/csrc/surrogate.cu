@@ -3,7 +3,7 @@
 // IonSolver src/kernels/sim_kernels.cl:940-955).
 //
 // Split of the reference's sum over the depth-D LOD bins of one cell:
-//   near : bins within Chebyshev distance RNEAR (= 2) of the cell's own bin
+//   near : bins within Chebyshev distance RNEAR (= 1) of the cell's own bin
 //          (own bin excluded, as the reference excludes it) -- summed exactly
 //          per cell (<= 124 terms instead of ~4095);
 //   far  : all other bins in range -- smooth over one block, so it is taken
@@ -560,7 +560,7 @@ __global__ void k_source_scale(const float* qu_lod, int V, int first, float* sca
 // ---------------------------------------------------------------------------
 constexpr uint32_t SC_CPT = 4, SC_THREADS = 256, SC_CELLS = SC_CPT * SC_THREADS;
 struct SurSmem {
-    FastSrc src[125];
+    FastSrc src[Surrogate::NEAR_CAND];
     float node[Surrogate::OUT_CH];
     // node values contracted along x: t1[lx][iy + 3 iz][c] = sum_ix wx_ix(lx) node[ix + 3 (iy + 3 iz)][c]
     float4 t1[Surrogate::MAX_BLOCK][9][2];
@@ -606,11 +606,12 @@ __global__ void __launch_bounds__(SC_THREADS, 2) k_surrogate_cells(const DevLbm 
         const uint32_t lane = threadIdx.x;
         const float4* qu = (const float4*)L.qu_lod;
         uint32_t cnt = 0;
-        for (int o0 = 0; o0 < 125; o0 += 32) {
+        constexpr int S = Surrogate::NEAR_SIDE, R = Surrogate::RNEAR;
+        for (int o0 = 0; o0 < Surrogate::NEAR_CAND; o0 += 32) {
             const int o = o0 + (int)lane;
-            const int x = bx + o % 5 - 2, y = by + (o / 5) % 5 - 2, z = bz + o / 25 - 2;
+            const int x = bx + o % S - R, y = by + (o / S) % S - R, z = bz + o / (S * S) - R;
             const int d = x + (y + z * nd) * nd;
-            const bool ok = o < 125 && x >= 0 && y >= 0 && z >= 0 && x < nd && y < nd && z < nd && d != (int)bin &&
+            const bool ok = o < Surrogate::NEAR_CAND && x >= 0 && y >= 0 && z >= 0 && x < nd && y < nd && z < nd && d != (int)bin &&
                             (uint32_t)d >= L.first_src;
             const uint32_t m = __ballot_sync(0xFFFFFFFFu, ok);
             if (ok) {  // coordinates relative to this bin's centre

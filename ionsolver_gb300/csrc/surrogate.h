@@ -16,7 +16,8 @@ int conv_tc_selftest(int nd, int cin, int cout, int dil, uint64_t seed, float* m
 
 class Surrogate {
 public:
-    static constexpr int RNEAR = 2;           // bins within this Chebyshev distance are summed exactly
+    static constexpr int RNEAR = 1;           // bins within this Chebyshev distance are summed exactly
+    static constexpr int NEAR_SIDE = 2 * RNEAR + 1, NEAR_CAND = NEAR_SIDE * NEAR_SIDE * NEAR_SIDE;
     static constexpr int NODES = 27;          // 3 x 3 x 3 interpolation nodes per block
     static constexpr int OUT_CH = NODES * 6;  // (Ex,Ey,Ez,Bx,By,Bz) per node
     static constexpr int OUT_PAD = 168;       // head channels: OUT_CH rounded up to 8 (the rest are zero)

@@ -22,7 +22,7 @@ from __future__ import annotations
 
 import numpy as np
 
-RNEAR = 2
+RNEAR = 1
 NODES = 27           # 3 x 3 x 3 interpolation nodes per block (offsets 0, (bs-1)/2, bs-1 on each axis)
 OUT_CH = NODES * 6   # (Ex, Ey, Ez, Bx, By, Bz) per node
 OUT_PAD = 168        # head channels (OUT_CH rounded up to 8; the rest have zero targets)
