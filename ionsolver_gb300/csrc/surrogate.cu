@@ -592,12 +592,13 @@ __device__ __forceinline__ void quad_weights(float t, float* w) {  // Lagrange w
     w[2] = 2.0f * t * (t - 0.5f);
 }
 
-__device__ __forceinline__ void surrogate_tile(const DevLbm& L, SurSmem& sm, uint32_t bin, int bx, int by, int bz,
-                                               uint32_t tile, uint32_t cells, const Magic& mx, const Magic& mxy);
+__device__ __forceinline__ void surrogate_tile(const DevLbm& L, SurSmem& sm, const float4* t2, uint32_t bin, int bx,
+                                               int by, int bz, uint32_t tile, uint32_t cells, const Magic& mx,
+                                               const Magic& mxy);
 
 __global__ void __launch_bounds__(SC_THREADS, 2) k_surrogate_cells(const DevLbm L, const float* Y, const float* G,
                                                                 const float* scales, float yE, float yB) {
-    extern __shared__ __align__(16) uint8_t sur_smem[];  // sizeof(SurSmem), above the 48 KB of static shared memory
+    extern __shared__ __align__(16) uint8_t sur_smem[];  // SurSmem, then the t2 table
     SurSmem& sm = *reinterpret_cast<SurSmem*>(sur_smem);
     const uint32_t bin = blockIdx.x;
     const int nd = (int)L.nd, V = nd * nd * nd;
@@ -652,14 +653,31 @@ __global__ void __launch_bounds__(SC_THREADS, 2) k_surrogate_cells(const DevLbm 
         sm.wyz[a][l] = make_float4(w[0], w[1], w[2], 0.0f);
     }
     __syncthreads();
+    // contracted along y as well: t2[(ly bsx + lx) 3 + iz][c] = sum_iy wy_iy(ly) t1[lx][iy + 3 iz][c],
+    // behind SurSmem in dynamic shared memory (bsx bsy 3 x 8 floats)
+    float4* t2 = reinterpret_cast<float4*>(sur_smem + sizeof(SurSmem));
+    for (uint32_t i = threadIdx.x; i < L.bsx * L.bsy * 24u; i += blockDim.x) {
+        const uint32_t c = i % 8u, iz = (i / 8u) % 3u, lx = (i / 24u) % L.bsx, ly = i / (24u * L.bsx);
+        const float4 wy = sm.wyz[0][ly];
+        float v = 0.0f;
+        if (c < 6u) {
+            const float* t = (const float*)&sm.t1[lx][0][0];
+            v = fmaf(wy.x, t[(0u + 3u * iz) * 8u + c], v);
+            v = fmaf(wy.y, t[(1u + 3u * iz) * 8u + c], v);
+            v = fmaf(wy.z, t[(2u + 3u * iz) * 8u + c], v);
+        }
+        ((float*)t2)[i] = v;
+    }
+    __syncthreads();
 
     const uint32_t cells = L.bsx * L.bsy * L.bsz;
     const Magic mx(L.bsx), mxy(L.bsx * L.bsy);
-    for (uint32_t tile = 0; tile * SC_CELLS < cells; tile++) surrogate_tile(L, sm, bin, bx, by, bz, tile, cells, mx, mxy);
+    for (uint32_t tile = 0; tile * SC_CELLS < cells; tile++) surrogate_tile(L, sm, t2, bin, bx, by, bz, tile, cells, mx, mxy);
 }
 
-__device__ __forceinline__ void surrogate_tile(const DevLbm& L, SurSmem& sm, uint32_t bin, int bx, int by, int bz,
-                                               uint32_t tile, uint32_t cells, const Magic& mx, const Magic& mxy) {
+__device__ __forceinline__ void surrogate_tile(const DevLbm& L, SurSmem& sm, const float4* t2, uint32_t bin, int bx,
+                                               int by, int bz, uint32_t tile, uint32_t cells, const Magic& mx,
+                                               const Magic& mxy) {
     // cell k of this thread: local index li -> (lx, ly, lz) in the bin, kept packed
     // (10 bits each) for the tail; flags are read now and used after the near sums
     float rx[SC_CPT], ry[SC_CPT], rz[SC_CPT];  // cell coordinates relative to the bin centre
@@ -718,16 +736,16 @@ __device__ __forceinline__ void surrogate_tile(const DevLbm& L, SurSmem& sm, uin
         const uint32_t m = (bx * L.bsx + lx) + ((by * L.bsy + ly) + (bz * L.bsz + lz) * L.ny) * L.nx;
         float e[3] = {0.0f, 0.0f, 0.0f}, b[3] = {0.0f, 0.0f, 0.0f};
         far_finish(cp[k / 2], fs[k / 2], (k & 1u) != 0, e, b);
-        // triquadratic interpolation: the x contraction is tabulated per bin (t1)
-        const float4 wy = sm.wyz[0][ly], wz = sm.wyz[1][lz];
-        const float wy3[3] = {wy.x, wy.y, wy.z}, wz3[3] = {wz.x, wz.y, wz.z};
+        // triquadratic interpolation: the x and y contractions are tabulated per bin (t2)
+        const float4 wz = sm.wyz[1][lz];
+        const float wz3[3] = {wz.x, wz.y, wz.z};
+        const float4* tc = t2 + (size_t)((ly * L.bsx + lx) * 3u) * 2u;
         float far[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll
-        for (int jk = 0; jk < 9; jk++) {
-            const float wgt = wy3[jk % 3] * wz3[jk / 3];
-            const float4 a = sm.t1[lx][jk][0], b2 = sm.t1[lx][jk][1];
-            far[0] = fmaf(wgt, a.x, far[0]); far[1] = fmaf(wgt, a.y, far[1]); far[2] = fmaf(wgt, a.z, far[2]);
-            far[3] = fmaf(wgt, a.w, far[3]); far[4] = fmaf(wgt, b2.x, far[4]); far[5] = fmaf(wgt, b2.y, far[5]);
+        for (int iz = 0; iz < 3; iz++) {
+            const float4 a = tc[2 * iz], b2 = tc[2 * iz + 1];
+            far[0] = fmaf(wz3[iz], a.x, far[0]); far[1] = fmaf(wz3[iz], a.y, far[1]); far[2] = fmaf(wz3[iz], a.z, far[2]);
+            far[3] = fmaf(wz3[iz], a.w, far[3]); far[4] = fmaf(wz3[iz], b2.x, far[4]); far[5] = fmaf(wz3[iz], b2.y, far[5]);
         }
         L.e_dyn[m] = sm.stat[0][slot] + L.ke * (e[0] + far[0]);
         L.e_dyn[N + m] = sm.stat[1][slot] + L.ke * (e[1] + far[1]);
@@ -887,7 +905,8 @@ int Surrogate::init(int nd, float bsx, float bsy, float bsz, int first_src) {
     rc |= alloc((void**)&bb_, (size_t)32 * V_ * 2);
     rc |= alloc((void**)&xb_, (size_t)16 * V_ * 2);
     if (rc) return ION_E_NOMEM;
-    if (cudaFuncSetAttribute(k_surrogate_cells, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SurSmem)) !=
+    if (cudaFuncSetAttribute(k_surrogate_cells, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(SurSmem) + (size_t)MAX_BLOCK * MAX_BLOCK * 96u)) !=
         cudaSuccess)
         return ION_E_CUDA;
     // far field of a unit charge in every source bin at the 27 nodes: the field of
@@ -1167,7 +1186,8 @@ void Surrogate::step(const DevLbm& L, cudaStream_t s, uint32_t salt) {
     k_source_scale<<<1, 256, 0, s>>>(L.qu_lod, V_, first_, scales_);
     k_pack_input_dev(L, s);
     infer_bf16(xin_, s);
-    k_surrogate_cells<<<L.n_bins, SC_THREADS, sizeof(SurSmem), s>>>(L, yout_, gunit_, scales_, yE_, yB_);
+    k_surrogate_cells<<<L.n_bins, SC_THREADS, sizeof(SurSmem) + (size_t)L.bsx * L.bsy * 96u, s>>>(L, yout_, gunit_,
+                                                                                                 scales_, yE_, yB_);
     k_sample_check<<<blocks_for((size_t)check_cells_ * 32, 128), 128, 0, s>>>(L, check_cells_, salt, stats_, counters_);
     k_sample_decide<<<1, 1, 0, s>>>(stats_, tol_, flag_, last_, counters_);
 }
