@@ -60,6 +60,16 @@ __device__ __forceinline__ void lod_bin_warp(const DevLbm& L, const uint32_t bin
     if (lane < 4u) L.qu_lod[(size_t)bin * 4u + lane] = acc;
 }
 
+// n / d by a multiply-high: floor(n m / 2^32) with m = floor((2^32 - 1) / d) + 1 (d > 1).
+// With n = q d + r, n m / 2^32 = n / d + n e / 2^32 with 0 <= e < 1, and n e / 2^32 < 1 / d
+// whenever n d < 2^32, so the floor is q (division by invariant integers, Granlund &
+// Montgomery 1994).  Callers keep n d < 2^32.
+struct Magic {
+    uint32_t d, m;
+    __device__ explicit Magic(uint32_t dd) : d(dd), m(dd > 1u ? 0xFFFFFFFFu / dd + 1u : 0u) {}
+    __device__ __forceinline__ uint32_t div(uint32_t n) const { return d > 1u ? __umulhi(n, m) : n; }
+};
+
 // LOD bins of one domain, one thread block per bin: warps 1..7 stream the
 // bin's cells (ascending cell index) through shared memory in slabs of
 // LB_SLAB cells, double-buffered, while lanes 0..3 of warp 0 add charge and
@@ -68,6 +78,7 @@ __device__ __forceinline__ void lod_bin_warp(const DevLbm& L, const uint32_t bin
 // -0.0f, which leaves every float (+0 included) unchanged under
 // round-to-nearest addition, so the sums need no branch and the summing
 // lanes read four cells per shared-memory load.
+
 constexpr uint32_t LB_THREADS = 256, LB_SLAB = 512;
 struct LodSmem {
     float v[2][4][LB_SLAB];  // [buffer][component][cell]
@@ -85,7 +96,9 @@ static __global__ void __launch_bounds__(LB_THREADS) k_lod_bins(const DevLbm L) 
     const uint32_t cells = L.bsx * L.bsy * L.bsz;
     const uint32_t nslabs = (cells + LB_SLAB - 1u) / LB_SLAB;
     const size_t N = L.n;
-    auto load = [&](uint32_t k) {  // warps 1..3; the slab is padded with -0.0f to a multiple of 4 cells
+    const Magic mx(L.bsx), mxy(L.bsx * L.bsy);
+    const bool magic = (uint64_t)cells * (L.bsx * L.bsy) < (1ull << 32);  // Magic's bound (bins of <= ~2^16 cells)
+    auto load = [&](uint32_t k) {  // warps 1..7; the slab is padded with -0.0f to a multiple of 4 cells
         const uint32_t base = k * LB_SLAB;
         const uint32_t cnt = min(LB_SLAB, cells - base);
         const uint32_t padded = (cnt + 3u) & ~3u;
@@ -95,7 +108,15 @@ static __global__ void __launch_bounds__(LB_THREADS) k_lod_bins(const DevLbm L) 
             float4 c = make_float4(-0.0f, -0.0f, -0.0f, -0.0f);
             if (i < cnt) {  // all five loads in flight at once; the flag selects afterwards
                 const uint32_t li = base + i;
-                const uint32_t lx = li % L.bsx, ly = (li / L.bsx) % L.bsy, lz = li / (L.bsx * L.bsy);
+                uint32_t lx, ly, lz;
+                if (magic) {
+                    lz = mxy.div(li);
+                    const uint32_t r = li - lz * mxy.d;
+                    ly = mx.div(r);
+                    lx = r - ly * mx.d;
+                } else {
+                    lx = li % L.bsx; ly = (li / L.bsx) % L.bsy; lz = li / (L.bsx * L.bsy);
+                }
                 const uint32_t n = (bx * L.bsx + lx) + ((by * L.bsy + ly) + (bz * L.bsz + lz) * L.ny) * L.nx;
                 const uint8_t f = L.flags[n];
                 const float4 a = make_float4(L.q[n], L.lod_cell[n], L.lod_cell[N + n], L.lod_cell[2 * N + n]);

@@ -571,15 +571,6 @@ struct SurSmem {
     uint32_t count;
 };
 
-// n / d for the cell indices of a bin (n < 32768, d <= 1024): floor(n m / 2^32) with
-// m = floor((2^32 - 1) / d) + 1.  With n = q d + r, n m / 2^32 = n / d + n e / 2^32,
-// 0 <= e < 1, and n e / 2^32 < n / 2^32 < 1 / d whenever n d < 2^32, so the floor is q
-// (division by invariant integers, Granlund & Montgomery 1994)
-struct Magic {
-    uint32_t d, m;
-    __device__ explicit Magic(uint32_t dd) : d(dd), m(dd > 1u ? 0xFFFFFFFFu / dd + 1u : 0u) {}
-    __device__ __forceinline__ uint32_t div(uint32_t n) const { return d > 1u ? __umulhi(n, m) : n; }
-};
 
 __device__ __forceinline__ void cp_async4(float* dst, const float* src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
