@@ -125,13 +125,14 @@ __device__ __forceinline__ void ep_load(const typename D::T* f, uint32_t N, uint
         v[i + 1] = D::ld(f, (size_t)(odd ? i + 1 : i) * N + j(i));
     }
 }
-template <class D, int Q, class NB>
+// IX: the type the slot offsets are computed in (uint32_t where Q N < 2^32 is known)
+template <class D, int Q, class NB, class IX = size_t>
 __device__ __forceinline__ void ep_store(typename D::T* f, uint32_t N, uint32_t n, bool odd, const NB& j, const float* v) {
     D::st(f, n, v[0]);
 #pragma unroll
     for (int i = 1; i < Q; i += 2) {
-        D::st(f, (size_t)(odd ? i + 1 : i) * N + j(i), v[i]);
-        D::st(f, (size_t)(odd ? i : i + 1) * N + n, v[i + 1]);
+        D::st(f, (IX)(odd ? i + 1 : i) * N + j(i), v[i]);
+        D::st(f, (IX)(odd ? i : i + 1) * N + n, v[i + 1]);
     }
 }
 
@@ -251,7 +252,7 @@ __device__ __forceinline__ float force_dir(const ForceState& s, int i) {
 
 // SRT collision + Esoteric-Pull store (sim_kernels.cl:714-723 / 649-656).
 // force: 0 = none (Fin = 0), 1 = Guo terms scaled by c_tau.
-template <class V, class D, class NB>
+template <class V, class D, class NB, class IX = size_t>
 __device__ __forceinline__ void srt_store(typename D::T* f, uint32_t N, uint32_t n, bool odd, const NB& j, const float* fh,
                                           const EqState& es, const ForceState& fs, bool force, float c_tau, float w,
                                           bool eqc) {
@@ -268,13 +269,13 @@ __device__ __forceinline__ void srt_store(typename D::T* f, uint32_t N, uint32_t
         const float Fb = force ? force_dir<V>(fs, i + 1) * c_tau : 0.0f;
         const float va = eqc ? fa : fmaf(1.0f - w, fh[i], fmaf(w, fa, Fa));
         const float vb = eqc ? fb : fmaf(1.0f - w, fh[i + 1], fmaf(w, fb, Fb));
-        D::st(f, (size_t)(odd ? i + 1 : i) * N + j(i), va);
-        D::st(f, (size_t)(odd ? i : i + 1) * N + n, vb);
+        D::st(f, (IX)(odd ? i + 1 : i) * N + j(i), va);
+        D::st(f, (IX)(odd ? i : i + 1) * N + n, vb);
     }
 }
 
 // TRT collision + store (sim_kernels.cl:725-754)
-template <class V, class D, class NB>
+template <class V, class D, class NB, class IX = size_t>
 __device__ __forceinline__ void trt_store(typename D::T* f, uint32_t N, uint32_t n, bool odd, const NB& j, const float* fh,
                                           const EqState& es, const ForceState& fs, bool force, float w, bool eqc) {
     const float wp = w, wm = 1.0f / (0.1875f / (1.0f / w - 0.5f) + 0.5f);
@@ -303,8 +304,8 @@ __device__ __forceinline__ void trt_store(typename D::T* f, uint32_t N, uint32_t
         const float ha = fh[i], hb = fh[i + 1];
         const float va = eqc ? ea : fmaf(0.5f * wp, ((ea - ha) + eb) - hb, fmaf(0.5f * wm, ((ea - eb) - ha) + hb, ha + Fa));
         const float vb = eqc ? eb : fmaf(0.5f * wp, ((eb - hb) + ea) - ha, fmaf(0.5f * wm, ((eb - ea) - hb) + ha, hb + Fb));
-        D::st(f, (size_t)(odd ? i + 1 : i) * N + j(i), va);
-        D::st(f, (size_t)(odd ? i : i + 1) * N + n, vb);
+        D::st(f, (IX)(odd ? i + 1 : i) * N + j(i), va);
+        D::st(f, (IX)(odd ? i : i + 1) * N + n, vb);
     }
 }
 
@@ -317,7 +318,7 @@ __device__ __forceinline__ float mag_v(const float* V, size_t N, uint32_t m) {
     return sqrtf((V[m] * V[m] + V[N + m] * V[N + m]) + V[2 * N + m] * V[2 * N + m]);
 }
 
-template <int Q, int FT, bool MHD, bool TRT, bool ECR = false, class SRC = GlobalSrc>
+template <int Q, int FT, bool MHD, bool TRT, bool ECR = false, class SRC = GlobalSrc, class IX = size_t>
 __device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const bool odd, const SRC& S = SRC{}) {
     using V = VSet<Q>;
     using D = Ddf<FT>;
@@ -397,7 +398,7 @@ __device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const
             uze = clampf(fmaf(efz, r2e, uze), -CS, CS);
             const ForceState fe = force_state<V>(uxe, uye, uze, efx, efy, efz);
             const EqState ee = eq_state(rhoe, uxe, uye, uze);
-            srt_store<V, D>((T*)L.ei, N, n, odd, j, ehn, ee, fe, true, c_tau, w, eqc);
+            srt_store<V, D, NbV<V>, IX>((T*)L.ei, N, n, odd, j, ehn, ee, fe, true, c_tau, w, eqc);
         }
         float fhn[Q];
         S.template load<D, Q>((const T*)L.fi, N, n, odd, j, fhn, LAT_FI);
@@ -424,7 +425,7 @@ __device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const
                 adv_equilibrium(rhoq, uxn, uyn, uzn, aeq);
 #pragma unroll
                 for (int i = 0; i < 7; i++) qhn[i] = fmaf(1.0f - L.wq, qhn[i], L.wq * aeq[i]);
-                ep_store<D, 7>((T*)L.fqi, N, n, odd, j7, qhn);
+                ep_store<D, 7, Nb7, IX>((T*)L.fqi, N, n, odd, j7, qhn);
             }
             L.q[n] = rhoq - rhoe;
             // Lorentz force on the gas
@@ -455,8 +456,8 @@ __device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const
         }
         const EqState es = eq_state(rhon, uxn, uyn, uzn);
         const ForceState fs = force_state<V>(uxn, uyn, uzn, fxn, fyn, fzn);
-        if constexpr (TRT) trt_store<V, D>((T*)L.fi, N, n, odd, j, fhn, es, fs, L.ext_vf, w, eqc);
-        else srt_store<V, D>((T*)L.fi, N, n, odd, j, fhn, es, fs, L.ext_vf, c_tau, w, eqc);
+        if constexpr (TRT) trt_store<V, D, NbV<V>, IX>((T*)L.fi, N, n, odd, j, fhn, es, fs, L.ext_vf, w, eqc);
+        else srt_store<V, D, NbV<V>, IX>((T*)L.fi, N, n, odd, j, fhn, es, fs, L.ext_vf, c_tau, w, eqc);
     }
 }
 
@@ -555,7 +556,7 @@ __global__ void __launch_bounds__(256, 2) k_sc_rows(const DevLbm L, const uint32
         const uint32_t y = r % ny, z = r / ny;
         for (uint32_t x = threadIdx.x; x < nx; x += blockDim.x) {
             const RowSrc<T> S{buf, nx, x, x + 1u == nx ? 0u : x + 1u, x == 0u ? nx - 1u : x - 1u, eb_off, fl_off};
-            sc_cell<19, FT, MHD, TRT, false, RowSrc<T>>(L, x + (y + z * ny) * nx, odd, S);
+            sc_cell<19, FT, MHD, TRT, false, RowSrc<T>, uint32_t>(L, x + (y + z * ny) * nx, odd, S);
         }
         __syncthreads();  // buffer b is free
     }
@@ -653,7 +654,7 @@ __global__ void __launch_bounds__(288, MHD ? 2 : 3) k_sc_rows_ws(const DevLbm L,
                 const uint32_t y = r % ny, z = r / ny;
                 for (uint32_t x = threadIdx.x; x < nx; x += nct) {
                     const RowSrc<T> S{buf, nx, x, x + 1u == nx ? 0u : x + 1u, x == 0u ? nx - 1u : x - 1u, eb_off, fl_off};
-                    sc_cell<19, FT, MHD, TRT, false, RowSrc<T>>(L, x + (y + z * ny) * nx, odd, S);
+                    sc_cell<19, FT, MHD, TRT, false, RowSrc<T>, uint32_t>(L, x + (y + z * ny) * nx, odd, S);
                 }
             }
             __syncwarp();
@@ -674,7 +675,8 @@ __global__ void __launch_bounds__(288, MHD ? 2 : 3) k_sc_rows_ws(const DevLbm L,
 // streams and two buffers fit in shared memory; false: use k_stream_collide
 template <int FT, bool MHD, bool TRT>
 bool launch_sc_rows(const DevLbm& L, uint32_t o, uint32_t* err, cudaStream_t s) {
-    if (L.nx % 16u || 2u * row_bytes<FT, MHD>(L.nx) > 200u * 1024u) return false;
+    // whole 16-byte rows, two buffers in shared memory, and 32-bit slot offsets (19 N < 2^32)
+    if (L.nx % 16u || 2u * row_bytes<FT, MHD>(L.nx) > 200u * 1024u || 19ull * L.n >= (1ull << 32)) return false;
     const uint32_t smem = 2u * row_bytes<FT, MHD>(L.nx);
     const bool ws = L.nx <= 256u;  // producer warp + one cell per thread and row
     const uint32_t threads =
