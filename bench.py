@@ -136,7 +136,7 @@ def bytes_per_lup(cfg: dict) -> int:
     return b
 
 
-def near_interactions(cfg: dict, flags: np.ndarray, rnear: int = 2) -> int:
+def near_interactions(cfg: dict, flags: np.ndarray, rnear: int) -> int:
     """Source terms the learned-far-field path sums exactly per step: fluid
     cells x bins within Chebyshev distance rnear of their own bin (own bin
     and bins below the source range excluded)."""
@@ -504,7 +504,7 @@ def main():
     if mhd:
         NAT.check(NAT.lib().ion_probe_fp32_peak(C.byref(tf)))
     if sur is not None:
-        inter = near_interactions(cfg0, doms[0].read("flags"))
+        inter = near_interactions(cfg0, doms[0].read("flags"), doms[0].SURROGATE_NEAR_RADIUS)
         avg = eb_ms / max(eb_n, 1)
         tflops = inter * FLOP_PER_INTERACTION / (avg * 1e-3) / 1e12
         roof_field = {"bound": "fp32", "achieved": tflops, "peak": tf.value, "unit": "TFLOP/s",

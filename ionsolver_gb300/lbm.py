@@ -395,6 +395,7 @@ class Lbm:
         return out
 
     SURROGATE_OUT = 168  # network output channels: 27 nodes x 6 components, padded to 168
+    SURROGATE_NEAR_RADIUS = 1  # bins within this Chebyshev distance of a cell's bin are summed exactly
 
     def _surrogate_count(self) -> int:
         # layer table of the network (4->32, 8 x 32->32, 32->168; 3^3 kernels)

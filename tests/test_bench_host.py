@@ -1,0 +1,64 @@
+"""Host-side logic of bench.py: which stencil kernel a workload runs, the
+algorithmic bytes per lattice update, workload-name parsing, and the source-term
+counts the field rooflines divide by (checked against a direct count)."""
+import types
+
+import numpy as np
+
+import bench
+from ionsolver_gb300 import workloads as W
+
+
+def test_stencil_kernel_names():
+    cfg = dict(velocity_set=2, n_x=128)
+    assert bench.stencil_kernel(cfg) == "k_sc_rows_ws"
+    assert bench.stencil_kernel(dict(cfg, n_x=384)) == "k_sc_rows"
+    assert bench.stencil_kernel(dict(cfg, n_x=24)) == "k_stream_collide"
+    assert bench.stencil_kernel(dict(cfg, ext_subgrid_ecr=1)) == "k_stream_collide"
+    assert bench.stencil_kernel(dict(cfg, velocity_set=1)) == "k_stream_collide"
+
+
+def test_bytes_per_lattice_update():
+    assert bench.bytes_per_lup(dict(float_type=2)) == 153
+    assert bench.bytes_per_lup(dict(float_type=2, update_fields=1)) == 169
+    mhd = dict(float_type=2, update_fields=1, ext_magneto_hydro=1, mhd_lod_depth=4)
+    assert bench.bytes_per_lup(mhd) == 417
+    assert bench.bytes_per_lup(dict(mhd, float_type=0)) == 237
+
+
+def test_workload_names(monkeypatch):
+    seen = []
+    monkeypatch.setattr(W, "mhd_box", lambda **kw: seen.append(kw) or {"config": {}})
+    a = types.SimpleNamespace(field_mode="surrogate", float_type="FP16S", workload="rings192d3")
+    bench.make_cases(a)
+    a.workload = "rings384"
+    bench.make_cases(a)
+    assert (seen[0]["n"], seen[0]["depth"], seen[0]["rings"]) == (192, 3, True)
+    assert (seen[1]["n"], seen[1]["depth"]) == (384, 4)
+
+
+def _bins(cfg):
+    D = int(cfg["mhd_lod_depth"])
+    nd = 1 << D
+    n_own = 1 + sum(8 ** (i + 1) for i in range(D))
+    return nd, n_own - nd ** 3
+
+
+def test_source_term_counts_against_a_direct_count():
+    case = W.mhd_box(n=32, depth=2, magnet_r=5.0, magnet_t=3.0)
+    cfg, flags = case["config"], case["fields"]["flags"].copy()
+    flags.reshape(32, 32, 32)[10:14, 8:20, 3:9] = 0x01  # an extra solid block
+    nd, first = _bins(cfg)
+    bs = 32 // nd
+    far = near = 0
+    for n in np.flatnonzero((flags & 0x1F) != 0x01):
+        x, y, z = n % 32, (n // 32) % 32, n // 1024
+        own = x // bs + (y // bs + z // bs * nd) * nd
+        for d in range(first, nd ** 3):
+            if d == own:
+                continue
+            far += 1
+            if max(abs(d % nd - x // bs), abs(d // nd % nd - y // bs), abs(d // (nd * nd) - z // bs)) <= 1:
+                near += 1
+    assert bench.field_interactions(cfg, flags) == far
+    assert bench.near_interactions(cfg, flags, 1) == near

@@ -79,3 +79,10 @@ def test_quadratic_weights_reproduce_quadratics():
         nodes = np.array([0.0, 0.5, 1.0])
         for f in (lambda u: 1 + 0 * u, lambda u: u, lambda u: 3 * u * u - u + 2):
             assert abs(w @ f(nodes) - f(t)) < 1e-12
+
+
+def test_near_radius_matches_the_library():
+    """The oracle's near radius (which the GPU targets are checked against) is the
+    one the Python mirror reports and bench.py counts near terms with."""
+    from ionsolver_gb300 import Lbm
+    assert S.RNEAR == Lbm.SURROGATE_NEAR_RADIUS
