@@ -706,8 +706,9 @@ bool launch_sc_rows(const DevLbm& L, uint32_t o, uint32_t* err, cudaStream_t s) 
         }
         per_sm = per_sm_of[v];
     }
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const uint32_t rows = L.ny * L.nz;
     const uint32_t grid = std::min<uint32_t>(rows, (uint32_t)(per_sm * sms));
     kern<<<grid, threads, smem, s>>>(L, o, err);
