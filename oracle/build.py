@@ -117,7 +117,7 @@ def variant_key(cfg: dict) -> str:
 def variant_header(cfg: dict) -> str:
     """The #define block of get_device_defines (src/lbm/domain.rs:736-858).
 
-    Sizes and unit constants become runtime values of the host driver; the
+    Sizes and unit constants become runtime values of the host program; the
     switches the kernel text tests with #if/#ifdef stay preprocessor
     literals."""
     vs = int(cfg.get("velocity_set", 2))

@@ -13,7 +13,7 @@
  *   ORC_REAL=double : the same formulas in double precision with double
  *                     storage (no 16-bit codecs): the FP64 accuracy oracle.
  *
- * Deliberate choices (all documented in the design doc):
+ * Deliberate choices:
  *   - LOD charge/velocity bins are accumulated in ascending cell order, the
  *     order a sequential run of the reference's float atomics produces
  *     (sim_kernels.cl:666-677); a GPU run of the reference has no fixed order.
@@ -591,7 +591,7 @@ static void field_update(orc* h) {
 }
 
 /* ------------------------------------------------------------------------
- * API (same C symbols as the reference-kernel driver, oracle/ref_shim)
+ * API (same C symbols as the reference-kernel host program, oracle/ref_shim)
  * ---------------------------------------------------------------------- */
 static void* xcalloc(size_t n, size_t s) { return n ? calloc(n, s) : NULL; }
 

@@ -1,6 +1,6 @@
 // ion_ref_host.cpp -- test infrastructure (oracle), not product code.
 //
-// Host driver around the reference's own kernels (IonSolver
+// Host program around the reference's own kernels (IonSolver
 // src/kernels/sim_kernels.cl, compiled as C++ through ion_ref_compat.hpp).
 // It restates, for one domain, the host orchestration of
 //   Lbm::new / LbmDomain::new  (src/lbm/mod.rs:166-210, src/lbm/domain.rs:88-212)
