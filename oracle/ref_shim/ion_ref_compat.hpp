@@ -16,7 +16,7 @@
 //     round-to-nearest-even binary32 -> binary16 (IEEE 754-2008 3.4, 4.3.1),
 //     written here from the format definition.
 //   - atomic_xchg on float: a sequentially consistent exchange of the bits.
-//   - get_global_id(0): a thread-local work-item index set by the driver.
+//   - get_global_id(0): a thread-local work-item index set by the host program.
 //   - printf inside kernels is compiled out.
 // The whole translation unit is compiled with -ffp-contract=off so that no
 // a*b+c is fused unless the kernel text itself calls fma().
