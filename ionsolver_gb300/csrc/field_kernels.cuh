@@ -241,7 +241,9 @@ __device__ __forceinline__ P2 fma2(P2 a, P2 b, P2 c) {
 
 // FAST far field in coordinates relative to an origin o near the cells (the
 // centre of their brick): with c' = c - o and p' = p - o,
-//   |R|^2 = (|c'|^2 + |p'|^2) - 2 c'.p'                 (4 operations, no R)
+//   |R|^2 = (|c'|^2 + |p'|^2) - 2 c'.p'                 (4 operations, no R,
+//         summed as (c'z mz + (c'x mx + |c'|^2)) + (c'y my + |p'|^2), m = -2 p':
+//         two independent chains, one dependent step fewer before the rsqrt)
 //   E = sum q R/|R|^3 = c' S - P,   S = sum q/|R|^3,  P = sum q p'/|R|^3
 //   B = sum qv x R/|R|^3 = A x c' - W,  A = sum qv/|R|^3,  W = sum (qv x p')/|R|^3
 // so one source costs 16 operations; |c'| is at most ~11 cells, which keeps
@@ -288,10 +290,8 @@ __device__ __forceinline__ void far_zero(FarSums& f) {
 __device__ __forceinline__ void far_fast2(const Pair3& c, P2 cc, const FastSrc& src, FarSums& f) {
     const ulonglong2* u = reinterpret_cast<const ulonglong2*>(src.d);
     const ulonglong2 d0 = u[0], d1 = u[1], d2 = u[2], d3 = u[3], d4 = u[4], d5 = u[5], d6 = u[6];
-    P2 r2 = add2(cc, d1.y);
-    r2 = fma2(c.x, d0.x, r2);
-    r2 = fma2(c.y, d0.y, r2);
-    r2 = fma2(c.z, d1.x, r2);
+    const P2 ra = fma2(c.z, d1.x, fma2(c.x, d0.x, cc)), rb = fma2(c.y, d0.y, d1.y);
+    const P2 r2 = add2(ra, rb);
     float i0, i1;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(i0) : "f"(lo32(r2)));
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(i1) : "f"(hi32(r2)));
@@ -313,10 +313,8 @@ __device__ __forceinline__ void far_fast2(const Pair3& c, P2 cc, const FastSrc& 
 // operations in the same order, for the source chunk that holds a cell's own bin
 __device__ __forceinline__ void far_fast1(const Pair3& c, P2 cc, const FastSrc& S, FarSums& f, bool hi) {
     const float4 d0 = S.d[0], d1 = S.d[1], d2 = S.d[2], d3 = S.d[3], d4 = S.d[4], d5 = S.d[5], d6 = S.d[6];
-    float r2 = half(cc, hi) + d1.z;
-    r2 = fmaf(half(c.x, hi), d0.x, r2);
-    r2 = fmaf(half(c.y, hi), d0.z, r2);
-    r2 = fmaf(half(c.z, hi), d1.x, r2);
+    const float ra = fmaf(half(c.z, hi), d1.x, fmaf(half(c.x, hi), d0.x, half(cc, hi))), rb = fmaf(half(c.y, hi), d0.z, d1.z);
+    const float r2 = ra + rb;
     float inv;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
     const float inv3 = (inv * inv) * inv;
