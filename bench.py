@@ -61,7 +61,7 @@ FLOP_PER_INTERACTION = 34  # one source's E and B: 34 FLOP + 1 sqrt (sim_kernels
 # (rings384: the 192^3 capture of the row-staged stencil scaled by the cell count, 8x; both
 # row forms copy the same streams per cell, so the traffic is proportional to the cells)
 NCU_TRAFFIC = {("tgv256", "k_sc_rows_ws"): 2.506631e9, ("mhd128", "k_sc_rows_ws"): 0.807230e9,
-               ("mhd128", "k_update_e_b_fast"): 64.611e6, ("rings384", "k_sc_rows"): 8 * 1.614150e9}
+               ("mhd128", "k_update_e_b_fast"): 64.001e6, ("rings384", "k_sc_rows"): 8 * 1.614150e9}
 
 
 def stencil_kernel(cfg: dict) -> str:
