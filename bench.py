@@ -11,8 +11,8 @@ Workloads (``--workload``; default ``mhd128``, the headline configuration):
       (seed 3), a disk magnet each (radius 4..12, seed 4), one persistent
       launch per step for all of them, autotuned launch shape, CUDA graph.
   rings384 : 384^3, FP16S storage, two coaxial ring magnets (R_out 48, R_in 32,
-      t 12, centres 128 apart, axis z; rings192 the same at half scale, for
-      profiling), LOD depth 4, the learned far field
+      t 12, centres 128 apart, axis z; rings192 and rings288 the same at 1/2 and
+      3/4 scale, for profiling), LOD depth 4, the learned far field
       (network trained before the timed region on 2000 exact snapshots, seed
       5) with the sampled exact check and device-decided exact fallback; the
       line also carries the exact FP32 step of the same box for comparison.
@@ -58,10 +58,10 @@ sys.path.insert(0, str(ROOT))
 FLOP_PER_INTERACTION = 34  # one source's E and B: 34 FLOP + 1 sqrt (sim_kernels.cl:950-954)
 # kernel-time results of one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum per launch);
 # the summaries with the commands that produced them are in profiles/
-# (rings384: the 192^3 capture of the row-staged stencil scaled by the cell count, 8x; both
-# row forms copy the same streams per cell, so the traffic is proportional to the cells)
+# (rings384: the rings288 capture of k_sc_rows scaled by the cell count, (384/288)^3; every
+# stream is read and written once per cell, so the traffic is proportional to the cells)
 NCU_TRAFFIC = {("tgv256", "k_sc_rows_ws"): 2.506631e9, ("mhd128", "k_sc_rows_ws"): 0.807230e9,
-               ("mhd128", "k_update_e_b_fast"): 64.001e6, ("rings384", "k_sc_rows"): 8 * 1.614150e9}
+               ("mhd128", "k_update_e_b_fast"): 64.001e6, ("rings384", "k_sc_rows"): 64 / 27 * 5.628695e9}
 
 
 def stencil_kernel(cfg: dict) -> str:
@@ -80,7 +80,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="mhd128",
-                   choices=["mhd128", "mhd256", "mhd64", "batch96", "rings384", "rings192", "rings192d3", "tgv64",
+                   choices=["mhd128", "mhd256", "mhd64", "batch96", "rings384", "rings192", "rings192d3", "rings288", "tgv64",
                             "tgv256", "tgv384"])
     p.add_argument("--field-mode", default=None, choices=["bitwise", "fast", "surrogate"],
                    help="default: surrogate for rings384, fast otherwise")
