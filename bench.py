@@ -47,6 +47,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -90,6 +91,7 @@ def parse():
     p.add_argument("--train-epochs", type=int, default=20)
     p.add_argument("--ref-seconds", type=float, default=20.0, help="CPU time budget of the reference/baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--clocks-dir", default=None, help="keep the raw nvidia-smi samples as clocks_rank<i>.csv here")
     p.add_argument("--no-e2e", action="store_true")
     a = p.parse_args()
     rings = a.workload.startswith("rings")
@@ -214,22 +216,31 @@ class Clocks:
              "clocks_event_reasons.sw_power_cap")
     NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
 
-    def __init__(self, index: int):
+    def __init__(self, index: int, keep_dir: str | None = None):
+        # the raw samples go to a temporary file unless --clocks-dir asks to keep them
         self.index = index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_rank{index}.csv"
+        self.keep = keep_dir is not None
+        self.path = (Path(keep_dir) / f"clocks_rank{index}.csv" if self.keep else
+                     Path(tempfile.gettempdir()) / f"ion_bench_clocks_{os.getpid()}_{index}.csv")
         self.t0 = self.t1 = None
 
     def start(self):
         try:
-            self.path.parent.mkdir(exist_ok=True)
+            self.path.parent.mkdir(parents=True, exist_ok=True)
             self.f = open(self.path, "w")
+        except OSError:
+            return
+        try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
                                           "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
             time.sleep(0.5)
-        except Exception:
+        except Exception:  # no nvidia-smi: no clock record
             self.proc = None
+            self.f.close()
+            if not self.keep:
+                self.path.unlink(missing_ok=True)
 
     def mark(self, which: str):
         setattr(self, which, _dt.datetime.now())
@@ -245,7 +256,10 @@ class Clocks:
             self.proc.kill()
         self.f.close()
         rows = []
-        for line in self.path.read_text().splitlines():
+        text = self.path.read_text()
+        if not self.keep:
+            self.path.unlink(missing_ok=True)
+        for line in text.splitlines():
             p = [x.strip() for x in line.split(",")]
             if len(p) < 8:
                 continue
@@ -441,7 +455,7 @@ def main():
     sur = None
     if a.field_mode == "surrogate":
         sur = surrogate_setup(a, cases[0], doms[0])
-    clocks = Clocks(dist.local)
+    clocks = Clocks(dist.local, a.clocks_dir)
     clocks.start()
 
     # ---- warm-up, then K timed steps (device time, CUDA events) -----------------

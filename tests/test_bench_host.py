@@ -1,6 +1,7 @@
 """Host-side logic of bench.py: which stencil kernel a workload runs, the
 algorithmic bytes per lattice update, workload-name parsing, and the source-term
-counts the field rooflines divide by (checked against a direct count)."""
+counts the field rooflines divide by (checked against a direct count), and the
+clock record of a line."""
 import types
 
 import numpy as np
@@ -62,3 +63,39 @@ def test_source_term_counts_against_a_direct_count():
                 near += 1
     assert bench.field_interactions(cfg, flags) == far
     assert bench.near_interactions(cfg, flags, 1) == near
+
+
+def _samples(rows):
+    return "".join(f"2026/01/01 00:00:{s:06.3f}, {mhz}, 2070, 900.0, {hw}, Not Active, Not Active, {cap}\n"
+                   for s, mhz, hw, cap in rows)
+
+
+def test_clock_summary_inside_the_timed_window(tmp_path):
+    """The clock record of a line: median SM clock and the throttle reasons seen in
+    the samples between the two marks (all samples when none fall inside)."""
+    import datetime as dt
+
+    class Done:  # stands in for the nvidia-smi process
+        def terminate(self): pass
+        def wait(self, t): pass
+
+    c = bench.Clocks(0, str(tmp_path))
+    c.path.write_text(_samples([(1.0, 1200, "Active", "Not Active"), (2.0, 2070, "Not Active", "Active"),
+                                (2.5, 2060, "Not Active", "Not Active"), (4.0, 900, "Active", "Not Active")]))
+    c.proc, c.f = Done(), open(tmp_path / "unused", "w")
+    c.t0, c.t1 = dt.datetime(2026, 1, 1, 0, 0, 1, 500000), dt.datetime(2026, 1, 1, 0, 0, 3)
+    r = c.stop()
+    assert (r["sm_mhz"], r["sm_max_mhz"], r["reasons"], r["samples"]) == (2065.0, 2070.0, ["sw_power_cap"], 2)
+    assert c.path.exists()  # kept: --clocks-dir was given
+
+
+def test_clock_samples_not_kept_by_default():
+    """Without --clocks-dir the raw samples live in a temporary file that is removed,
+    also when nvidia-smi cannot be started (no record at all, as on a host without GPU)."""
+    c = bench.Clocks(0)
+    c.start()
+    if c.proc is None:
+        assert c.stop() is None
+    else:
+        c.mark("t0"); c.mark("t1"); c.stop()
+    assert not c.path.exists()
