@@ -182,23 +182,6 @@ __device__ __forceinline__ void add_src(float rx, float ry, float rz, float4 val
     }
 }
 
-// FAST far field of one source: E += q R/|R|^3 and, for B, the two sums
-// A += qv/|R|^3 and W += (qv x p)/|R|^3, from which B = A x c - W at the end
-// (qv x (c - p) = qv x c - qv x p): 3 FMA per source instead of 9.
-// p = (px, py, pz, q), qv = (q vx, q vy, q vz, -), w = qv x p.
-__device__ __forceinline__ void far_fast(float cx, float cy, float cz, float4 p, float4 qv, float4 w, float* e, float* A,
-                                         float* W) {
-    const float rx = cx - p.x, ry = cy - p.y, rz = cz - p.z;
-    const float r2 = fmaf(rz, rz, fmaf(ry, ry, rx * rx));
-    float inv;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
-    const float inv3 = inv * inv * inv;
-    const float s = p.w * inv3;
-    e[0] = fmaf(s, rx, e[0]); e[1] = fmaf(s, ry, e[1]); e[2] = fmaf(s, rz, e[2]);
-    A[0] = fmaf(inv3, qv.x, A[0]); A[1] = fmaf(inv3, qv.y, A[1]); A[2] = fmaf(inv3, qv.z, A[2]);
-    W[0] = fmaf(inv3, w.x, W[0]); W[1] = fmaf(inv3, w.y, W[1]); W[2] = fmaf(inv3, w.z, W[2]);
-}
-
 // Packed FP32 pairs (PTX add/mul/fma .f32x2, sm_100 and later): one
 // instruction does the same IEEE round-to-nearest operation on the two
 // halves of a 64-bit register, so two cells advance through one source with

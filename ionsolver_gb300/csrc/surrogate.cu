@@ -201,11 +201,6 @@ __global__ void k_mse(const float* y, const float* t, float* g, float* loss, siz
     if (threadIdx.x == 0) atomicAdd(loss, red[0]);
 }
 
-__global__ void k_add(float* a, const float* b, size_t n) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) a[i] += b[i];
-}
-
 // Adam (Kingma & Ba 2015) with bias correction
 __global__ void k_adam(float* w, const float* g, float* m, float* v, size_t n, float lr, float b1, float b2, float eps,
                        float c1, float c2) {
