@@ -194,6 +194,8 @@ __device__ __forceinline__ P2 pk(float lo, float hi) {
     asm("mov.b64 %0, {%1,%2};" : "=l"(r) : "f"(lo), "f"(hi));
     return r;
 }
+// (the unpack writes both halves; the unused one draws warning 550)
+#pragma nv_diag_suppress 550
 __device__ __forceinline__ float lo32(P2 v) {
     float a, b;
     asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
@@ -204,6 +206,7 @@ __device__ __forceinline__ float hi32(P2 v) {
     asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
     return b;
 }
+#pragma nv_diag_default 550
 __device__ __forceinline__ float half(P2 v, bool hi) { return hi ? hi32(v) : lo32(v); }
 __device__ __forceinline__ void set_half(P2& v, bool hi, float x) { v = hi ? pk(lo32(v), x) : pk(x, hi32(v)); }
 __device__ __forceinline__ P2 add2(P2 a, P2 b) {

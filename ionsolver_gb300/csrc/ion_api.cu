@@ -403,7 +403,6 @@ struct Reader {
     bool need(size_t n) { if (pos + n > b.size()) ok = false; return ok; }
     uint8_t u8() { if (!need(1)) return 0; return b[pos++]; }
     uint32_t u32() { if (!need(4)) return 0; uint32_t v = 0; for (int i = 0; i < 4; i++) v |= (uint32_t)b[pos++] << (8 * i); return v; }
-    uint64_t u64() { if (!need(8)) return 0; uint64_t v = 0; for (int i = 0; i < 8; i++) v |= (uint64_t)b[pos++] << (8 * i); return v; }
     float f32() { const uint32_t u = u32(); float f; memcpy(&f, &u, 4); return f; }
 };
 void push32(std::vector<unsigned char>& v, uint32_t x) { for (int i = 0; i < 4; i++) v.push_back((unsigned char)(x >> (8 * i))); }

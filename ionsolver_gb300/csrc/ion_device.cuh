@@ -66,7 +66,9 @@ template <> struct VSet<9> {
 // ---------------------------------------------------------------------------
 struct FastDiv {
     uint32_t d, m, l;
-    FastDiv() : d(1), m(1), l(0) {}
+    // trivial, so DevLbm can live in __shared__; a zero-initialised FastDiv
+    // (m = 0, l = 0) returns n, i.e. divides by 1
+    FastDiv() = default;
     explicit FastDiv(uint32_t div) : d(div) {
         l = 0;
         while ((1ull << l) < div) l++;
