@@ -1,0 +1,90 @@
+"""Known-answer checks of the oracle against physics (CPU).  The CUDA path is held
+bit-identical to this oracle by the GPU parity tests, so these pin it as well.
+
+* Equilibrium moments: the equilibrium of calculate_f_eq (sim_kernels.cl:155-207)
+  carries the density and velocity it was built from, sum f_eq = rho and
+  sum c f_eq = rho u (calculate_rho_u, sim_kernels.cl:208-233).  With uniform rho and u,
+  streaming leaves every cell's distribution unchanged, so the moments that
+  update_fields reads right after initialize (sim_kernels.cl:760-859) are those of the
+  stored equilibrium itself.
+* Viscosity: a shear wave u_x = A cos(kx) sin(ky), u_y = -A sin(kx) cos(ky) decays as
+  exp(-2 nu k^2 t) in the low-Mach limit.  The relaxation rate is
+  w = 1 / (3 nu + 1/2) (domain.rs:808), and TRT's "-" rate follows from the magic
+  parameter 3/16 (sim_kernels.cl:724-726), so both collisions relax shear at nu.
+* Mass and momentum: stream + collide conserve both; the wave has zero net momentum.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from ionsolver_gb300 import workloads as W
+
+# (rho, u) pairs, |u| up to ~0.14 lattice units
+UNIFORM = [(1.0, (0.0, 0.0, 0.0)), (1.0, (0.05, -0.02, 0.01)), (1.3, (0.1, 0.0, -0.08)), (0.8, (-0.12, 0.07, 0.03))]
+
+
+def _oracle(kind, velocity_set, shape, relaxation_time=0):
+    nx, ny, nz = shape
+    cfg = O.make_config(velocity_set=velocity_set, relaxation_time=relaxation_time, float_type=2, n_x=nx, n_y=ny,
+                        n_z=nz, nu=W.NU_1_30, update_fields=1)
+    return O.OracleLbm(cfg, kind, 1)
+
+
+@pytest.mark.parametrize("kind", ["f32", "f64"])
+@pytest.mark.parametrize("velocity_set,shape", [(2, (4, 4, 4)), (1, (4, 4, 4)), (0, (4, 4, 1))],
+                         ids=["D3Q19", "D3Q15", "D2Q9"])
+def test_equilibrium_moments(kind, velocity_set, shape):
+    n = shape[0] * shape[1] * shape[2]
+    real = np.float32 if kind == "f32" else np.float64
+    # two ulps of the largest velocity component
+    tol = 2.0 * float(np.spacing(real(0.12)))
+    for rho, (ux, uy, uz) in UNIFORM:
+        if velocity_set == 0:
+            uz = 0.0
+        o = _oracle(kind, velocity_set, shape)
+        o.set_field("u", np.concatenate([np.full(n, ux), np.full(n, uy), np.full(n, uz)]))
+        o.set_field("rho", np.full(n, rho))
+        o.initialize()
+        o.field("u")[:] = 0
+        o.field("rho")[:] = 0
+        o.update_fields()
+        r = o.field("rho")[:n].astype(np.float64)
+        u = o.field("u")[:3 * n].astype(np.float64).reshape(3, n)
+        assert np.all(r == float(real(rho))), (rho, np.max(np.abs(r - float(real(rho)))))
+        want = np.array([ux, uy, uz], real).astype(np.float64)[:, None]
+        assert np.max(np.abs(u - want)) <= tol, (rho, (ux, uy, uz), np.max(np.abs(u - want)))
+        o.close()
+
+
+@pytest.mark.parametrize("kind", ["f32", "f64"])
+@pytest.mark.parametrize("relaxation_time", [0, 1], ids=["SRT", "TRT"])
+def test_shear_wave_decays_at_the_viscosity(kind, relaxation_time):
+    nx, ny, nz = 32, 32, 4
+    n = nx * ny * nz
+    amp0, k = 0.01, 2.0 * np.pi / nx
+    z, y, x = np.meshgrid(np.arange(nz) + 0.5, np.arange(ny) + 0.5, np.arange(nx) + 0.5, indexing="ij")
+    mode = np.cos(k * x) * np.sin(k * y)
+    ux, uy = amp0 * mode, -amp0 * np.sin(k * x) * np.cos(k * y)
+    o = _oracle(kind, 2, (nx, ny, nz), relaxation_time)
+    o.set_field("u", np.concatenate([ux.ravel(), uy.ravel(), np.zeros(n)]))
+    o.set_field("rho", np.ones(n))
+    o.initialize()
+
+    def amplitude():
+        u = o.field("u")[:n].astype(np.float64).reshape(nz, ny, nx)
+        return float(np.sum(u * mode) / np.sum(mode * mode))
+
+    # the uniform initial density launches a weak acoustic transient: measure after it
+    o.run(100)
+    t0, a0 = o.time_step, amplitude()
+    o.run(300)
+    t1, a1 = o.time_step, amplitude()
+    rate = np.log(a1 / a0) / (t1 - t0)
+    expected = -2.0 * W.NU_1_30 * k * k
+    assert abs(rate / expected - 1.0) < 5e-3, (rate, expected)
+    rho = o.field("rho")[:n].astype(np.float64)
+    mom = rho * o.field("u")[:n].astype(np.float64)
+    eps = 1e-5 if kind == "f32" else 1e-12  # rounding over 400 steps, relative to the sums' scale
+    assert abs(rho.sum() - n) < eps * n
+    assert abs(mom.sum()) < eps * np.abs(mom).sum()
+    o.close()
