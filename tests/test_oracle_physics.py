@@ -12,12 +12,20 @@ bit-identical to this oracle by the GPU parity tests, so these pin it as well.
   w = 1 / (3 nu + 1/2) (domain.rs:808), and TRT's "-" rate follows from the magic
   parameter 3/16 (sim_kernels.cl:724-726), so both collisions relax shear at nu.
 * Mass and momentum: stream + collide conserve both; the wave has zero net momentum.
+* Magnet field: psi_from_mesh sums one point dipole per magnet cell,
+  psi = sum M.(r - r')/|r - r'|^3 / (4 pi) (sim_kernels.cl:1234-1251), and
+  static_b_from_mesh takes B = -KMU0 grad psi by central differences
+  (sim_kernels.cl:1253-1276).  On the axis of a voxelised disk the result is checked
+  against the exact field of the same dipoles, and against the uniformly magnetised
+  cylinder, B = mu0 M / 2 [(s + t/2) / sqrt((s + t/2)^2 + R^2) - (s - t/2) / sqrt((s - t/2)^2 + R^2)],
+  with R the radius of a disk of the voxelised volume.
 """
 import numpy as np
 import pytest
 
 import oracle as O
 from ionsolver_gb300 import workloads as W
+from ionsolver_gb300.meshes import cylinder
 
 # (rho, u) pairs, |u| up to ~0.14 lattice units
 UNIFORM = [(1.0, (0.0, 0.0, 0.0)), (1.0, (0.05, -0.02, 0.01)), (1.3, (0.1, 0.0, -0.08)), (0.8, (-0.12, 0.07, 0.03))]
@@ -87,4 +95,46 @@ def test_shear_wave_decays_at_the_viscosity(kind, relaxation_time):
     eps = 1e-5 if kind == "f32" else 1e-12  # rounding over 400 steps, relative to the sums' scale
     assert abs(rho.sum() - n) < eps * n
     assert abs(mom.sum()) < eps * np.abs(mom).sum()
+    o.close()
+
+
+def test_disk_magnet_field_on_axis():
+    n, radius, thick = 48, 8.0, 4.0
+    case = W.mhd_box(n=n, float_type=2, depth=2)
+    cfg = O.make_config(**case["config"])
+    mu0 = float(O.constants(cfg).kmu0)
+    o = O.OracleLbm(cfg, "f32", O.cpu_count())
+    o._threads()
+    for name, arr in case["fields"].items():
+        o.set_field(name, arr)
+    o.voxelise(*cylinder((0.5 * n, 0.5 * n, 0.5 * n), radius, thick, axis=2), "magnet", (0.0, 0.0, W.MAGNETIZATION_SI))
+    N = n ** 3
+    m_field = o.field("b_dyn")[:3 * N].reshape(3, n, n, n).astype(np.float64).copy()  # M, before precompute_b
+    o.precompute_b()
+    b = o.field("b_stat")[:3 * N].reshape(3, n, n, n).astype(np.float64)
+    mz, my, mx = np.nonzero(m_field[2])
+    m = m_field[2][mz, my, mx]
+    assert m.size > 0 and np.all(m == m[0]) and not m_field[:2].any()  # uniform, along the axis
+    src = np.stack([mx, my, mz], 1).astype(np.float64)
+    centre = src.mean(0)
+    r_eff = np.sqrt(m.size / (np.pi * thick))
+    ix, iy = int(round(centre[0])), int(round(centre[1]))
+
+    def dipoles(p):  # B_z of the magnet cells as point dipoles
+        r = p[None, :] - src
+        d = np.linalg.norm(r, axis=1)
+        return mu0 / (4.0 * np.pi) * np.sum(m * (3.0 * r[:, 2] ** 2 / d ** 2 - 1.0) / d ** 3)
+
+    def cylinder_axis(s):
+        a, c = s + 0.5 * thick, s - 0.5 * thick
+        return 0.5 * mu0 * m[0] * (a / np.hypot(a, r_eff) - c / np.hypot(c, r_eff))
+
+    checked = 0
+    for z in range(int(np.ceil(centre[2] + 5.0)), n - 2):
+        s = z - centre[2]
+        bz = b[2, z, iy, ix]
+        assert abs(bz / dipoles(np.array([ix, iy, z], float)) - 1.0) < 1e-2, (s, bz)
+        assert abs(bz / cylinder_axis(s) - 1.0) < (4e-2 if s < 14.0 else 1e-2), (s, bz)
+        checked += 1
+    assert checked >= 15
     o.close()
