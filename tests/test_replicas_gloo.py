@@ -1,6 +1,6 @@
 """The N>1 benchmark path is replicas only (each rank advances its own
-domain); its host-side plumbing -- barrier and max-over-ranks timing -- runs
-here as two gloo ranks on the CPU."""
+domain); its host-side plumbing -- barrier and max-over-ranks timing, and the
+reference arm's rank-0-only line -- runs here as two gloo ranks on the CPU."""
 import os
 import socket
 
@@ -42,3 +42,27 @@ def test_two_rank_max_over_ranks():
         assert p.exitcode == 0
     res = dict(q.get(timeout=10) for _ in range(2))
     assert res == {0: 15.0, 1: 15.0}
+
+
+def test_reference_arm_prints_one_line_from_rank_zero():
+    """`bench.py --impl reference` under torchrun with two ranks: rank 0 times the
+    reference's kernels on the host cores and prints the one contract line; rank 1
+    exits 0 without work."""
+    import json
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parents[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
+           "127.0.0.1", "--master-port", str(_free_port()), str(root / "bench.py"), "--impl", "reference",
+           "--workload", "mhd64", "--gpus", "2", "--steps", "1", "--warmup", "3", "--ref-seconds", "1"]
+    r = subprocess.run(cmd, cwd=root, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(s) for s in r.stdout.splitlines() if s.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = lines[0]
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["unit"] == "MLUPs/s" and d["value"] > 0
+    assert d["cpu_baseline"]["kind"] in ("reference", "port") and d["cpu_baseline"]["value"] == d["value"]
+    assert d["e2e"] == {"value": d["value"], "unit": "MLUPs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["config"]["workload"] == "mhd64"
