@@ -44,7 +44,8 @@ def test_abi_version_and_defaults():
     (dict(d_x=2), -2), (dict(velocity_set=3), -2), (dict(velocity_set=0, n_z=4), -2),
     (dict(ext_magneto_hydro=1), -2), (dict(ext_magneto_hydro=1, ext_volume_force=1, n_x=20), -2),
     (dict(ext_subgrid_ecr=1), -2), (dict(n_x=0), -2), (dict(float_type=7), -2),
-    (dict(ext_magneto_hydro=1, ext_volume_force=1, mhd_lod_depth=5), -2)])
+    (dict(ext_magneto_hydro=1, ext_volume_force=1, mhd_lod_depth=5), -2),
+    (dict(n_x=2048, n_y=2048, n_z=1024), -2), (dict(n_x=65536, n_y=65536, n_z=1), -2)])
 def test_create_rejects_configs(change, code):
     c = I.LbmConfig(velocity_set=2, n_x=32, n_y=32, n_z=32, float_type=2)
     for k, v in change.items():
@@ -79,3 +80,15 @@ def test_null_arguments_are_errors():
     assert lib.ion_lbm_initialize(None) == -1
     assert lib.ion_lbm_run(None, 3) == -1
     assert lib.ion_config_default(None) == -1
+
+
+def test_create_without_a_device_is_an_error_not_an_abort():
+    """A valid configuration on a host without a usable CUDA device: ION_E_CUDA and a
+    message (the reference exits the process instead, opencl.rs:11-13)."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    c = I.LbmConfig(velocity_set=2, n_x=1024, n_y=1024, n_z=1024, float_type=2)
+    h = C.c_void_p()
+    assert N.lib().ion_lbm_create(C.byref(c.to_c()), C.byref(h)) == -3 and not h.value
+    assert b"CUDA" in N.lib().ion_last_error()
