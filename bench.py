@@ -6,7 +6,14 @@ Workloads (``--workload``; default ``mhd128``, the headline configuration):
       storage (``--float-type`` for FP16S/FP16C), tau 0.6, one-cell solid walls,
       charge U[-1e-3,1e-3] (seed 1), velocity N(0,1e-3^2) (seed 2), an axially
       magnetised disk magnet (r 16, t 8 at 128^3) on the z = 1 face, LOD depth
-      4, the exact LOD E/B update every step.
+      4, the exact LOD E/B update every step.  ``--start plasma`` (default for
+      every MHD workload): the finite-plasma start of workloads.mhd_plasma
+      (electron gas at a background density in units where the state stays
+      finite); ``--start reference``: the reference's start, whose electron
+      gas is empty and turns every MHD field NaN within a few steps.
+      The mhd128 line also carries a ``surrogate`` record: the rings384
+      workload below (training, step-1 field error, timed learned-field steps,
+      fallbacks) against the exact FP32 step of the same box.
   batch96 : 96 independent MHD domains, cube edges from {32,48,64,80,96}
       (seed 3), a disk magnet each (radius 4..12, seed 4), one persistent
       launch per step for all of them, autotuned launch shape, CUDA graph.
@@ -93,6 +100,11 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--clocks-dir", default=None, help="keep the raw nvidia-smi samples as clocks_rank<i>.csv here")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--start", default="plasma", choices=["plasma", "reference"],
+                   help="initial electron gas of the MHD workloads (see the module docstring)")
+    p.add_argument("--no-surrogate-record", action="store_true",
+                   help="mhd128: leave out the learned-far-field record (rings384)")
+    p.add_argument("--surrogate-size", type=int, default=384, help="box edge of the mhd128 line's surrogate record")
     a = p.parse_args()
     rings = a.workload.startswith("rings")
     a.field_mode = a.field_mode or ("surrogate" if rings else "fast")
@@ -111,14 +123,17 @@ def make_cases(a) -> list[dict]:
     fm = FM[a.field_mode]
     ft = FT[a.float_type]
     w = a.workload
+    plasma = a.start == "plasma"
     if w == "batch96":
-        return W.batch_domains(96, float_type=ft, field_mode=fm)
+        return W.batch_domains(96, float_type=ft, field_mode=fm, plasma=plasma)
     if w.startswith("rings"):  # rings192: the same box at half the size; rings192d3: LOD depth 3, i.e. the
         n, _, d = w[5:].partition("d")  # 24^3-cell bins of rings384 (profiling cases)
-        return [W.mhd_box(n=int(n), float_type=ft, depth=int(d or 4), field_mode=fm, rings=True)]
+        case = W.mhd_box(n=int(n), float_type=ft, depth=int(d or 4), field_mode=fm, rings=True)
+        return [W.to_plasma(case) if plasma else case]
     n = int(w[3:])
     if w.startswith("mhd"):
-        return [W.mhd_box(n=n, float_type=ft, field_mode=fm, magnet_r=16.0 * n / 128, magnet_t=8.0 * n / 128)]
+        case = W.mhd_box(n=n, float_type=ft, field_mode=fm, magnet_r=16.0 * n / 128, magnet_t=8.0 * n / 128)
+        return [W.to_plasma(case) if plasma else case]
     case = W.taylor_green(n=n, amplitude=0.05, float_type=ft)
     case["config"]["update_fields"] = 0
     return [case]
@@ -289,29 +304,62 @@ def cpu_sample_cases(a, cases: list[dict]) -> list[dict]:
 
 
 # ---------------------------------------------------------------------------
-def cpu_run(cases: list[dict], steps: int, budget_s: float, init_fields: list[dict] | None):
-    """Advances the cases on the host cores within a time budget.
-
-    Returns (MLUPs/s, sample description, kind, cores)."""
+def _oracle_for(case: dict, kind: str, cores: int, init: dict):
+    """An initialized CPU oracle of the case ("ref": the reference's kernels,
+    "f32": the restatement), with the case's start.  The reference's kernels
+    have no finite-plasma start, so for them the electron and charge DDFs
+    after initialize come from the restatement's initialize of the same
+    fields (the reference's calculate_f_eq / calculate_a_eq at rho_e0 and
+    Q + rho_e0)."""
     import oracle as O
     from tests import _util as U
-    cores = O.cpu_count()
-    kind = "reference" if O.reference_available() else "port"
-    done_cells, done_steps, t_total, used = 0, 0, 0.0, 0
-    for i, case in enumerate(cases):
-        try:
-            o = O.OracleLbm(U.oracle_config(case), "ref" if kind == "reference" else "f32", cores)
-        except Exception:
-            kind = "port"
-            o = O.OracleLbm(U.oracle_config(case), "f32", cores)
+
+    def make(k):
+        o = O.OracleLbm(U.oracle_config(case), k, cores)
         for name, arr in case["fields"].items():
             o.set_field(name, arr)
-        for name, arr in ((init_fields or [{}] * len(cases))[i] or {}).items():  # static fields (setup, untimed)
+        for name, arr in init.items():  # static fields (setup, untimed)
             o.set_field(name, arr)
-        o.initialize()
+        return o
+    o = make(kind)
+    rho_e0 = case.get("electron_background")
+    if rho_e0 and kind != "ref":
+        o.set_electron_background(rho_e0)
+    o.initialize()
+    if rho_e0 and kind == "ref":
+        r = make("f32")
+        r.set_electron_background(rho_e0)
+        r.initialize()
+        for name in ("ei", "fqi"):
+            o.set_field(name, r.field(name))
+        r.close()
+    return o
+
+
+def cpu_run(cases: list[dict], steps: int, budget_s: float, init_fields: list[dict] | None, warmup: int = 0):
+    """Advances the cases on the host cores: `warmup` untimed steps of the
+    first case, then timed steps until `steps` are done or the time budget is
+    spent (a step that starts inside the budget is finished).
+
+    Returns (MLUPs/s, sample description, kind, cores, timed steps, warm-up steps)."""
+    import oracle as O
+    cores = O.cpu_count()
+    kind = "reference" if O.reference_available() else "port"
+    done_cells, done_steps, t_total, used, warm = 0, 0, 0.0, 0, 0
+    for i, case in enumerate(cases):
+        init = (init_fields or [{}] * len(cases))[i] or {}
+        try:
+            o = _oracle_for(case, "ref" if kind == "reference" else "f32", cores, init)
+        except Exception:
+            kind = "port"
+            o = _oracle_for(case, "f32", cores, init)
+        if i == 0:
+            for _ in range(warmup):
+                o.do_time_step()
+                warm += 1
         t0 = time.perf_counter()
         s = 0
-        while s < steps:
+        while done_steps + s < steps:
             o.do_time_step()
             s += 1
             if t_total + time.perf_counter() - t0 > budget_s:
@@ -321,16 +369,16 @@ def cpu_run(cases: list[dict], steps: int, budget_s: float, init_fields: list[di
         done_steps += s
         used += 1
         o.close()
-        if t_total > budget_s:
+        if t_total > budget_s or done_steps >= steps:
             break
     mlups = done_cells / t_total / 1e6
     if len(cases) == 1:
         c = cases[0]["config"]
-        sample = (f"{done_steps} full timestep(s) of the {c['n_x']}x{c['n_y']}x{c['n_z']} case after initialize, "
-                  f"{t_total:.1f} s")
+        sample = (f"{done_steps} full timestep(s) of the {c['n_x']}x{c['n_y']}x{c['n_z']} case after initialize"
+                  f"{' and ' + str(warm) + ' untimed warm-up step(s)' if warm else ''}, {t_total:.1f} s")
     else:
         sample = f"{done_steps} domain-step(s) over the first {used} of {len(cases)} domains, {t_total:.1f} s"
-    return mlups, sample, kind, cores
+    return mlups, sample, kind, cores, done_steps, warm
 
 
 # ---------------------------------------------------------------------------
@@ -405,6 +453,47 @@ def exact_fp32_step(case: dict, src) -> dict:
             "exact_fp32_steps_timed": steps}
 
 
+def surrogate_record(a) -> dict:
+    """Configuration 4 inside the headline line: the two-ring box at
+    --surrogate-size with FP16S storage and the learned far field.  Trains the
+    network (untimed setup), measures the step-1 field error against the exact
+    sum of the same state, times learned-field steps (CUDA events, graph
+    replay) with the sampled check and fallback active, and times the exact
+    FP32 step of the same box."""
+    import ionsolver_gb300 as I
+    from ionsolver_gb300 import workloads as W
+    n = a.surrogate_size
+    case = W.mhd_box(n=n, float_type=0, depth=4, field_mode=2, rings=True)
+    if a.start == "plasma":
+        case = W.to_plasma(case)
+    lbm = I.Lbm(W.lbm_config(case))
+    W.apply_case(lbm, case)
+    lbm.initialize()
+    rec = surrogate_setup(a, case, lbm)
+    warm, steps = 3, 20
+    for _ in range(warm):
+        lbm.do_time_step()
+    lbm.finish_queues(600000)
+    lbm.record_event(0)
+    lbm.run(steps)
+    lbm.record_event(1)
+    ms = lbm.elapsed_ms(0, 1)
+    lbm.finish_queues(600000)
+    st = lbm.surrogate_stats()
+    cells = n ** 3
+    rec.update(workload=f"rings{n}", float_type="FP16S", steps_timed=steps, warmup=warm,
+               ms_per_step=ms / steps, mlups=cells * steps / (ms * 1e-3) / 1e6,
+               checks_in_run=st["checks"], fallbacks_in_run=st["fallbacks"],
+               nonfinite_checks_in_run=st["nonfinite"], last_check_err_e=st["err_e"], last_check_err_b=st["err_b"])
+    u = lbm.read("u")
+    rec["state_finite_after_run"] = bool(np.isfinite(u).all() and np.isfinite(lbm.read("e_dyn")).all())
+    rec.update(exact_fp32_step(case, lbm))
+    rec["speedup_vs_exact_fp32"] = rec["exact_fp32_ms_per_step"] / rec["ms_per_step"]
+    rec["targets"] = {"speedup_vs_exact_fp32": ">= 2", "field_rel_err_step1": "<= 1e-2"}
+    lbm.close()
+    return rec
+
+
 def main():
     a = parse()
     dist = Dist()
@@ -421,6 +510,10 @@ def main():
                     "update_fields": bool(cfg0.get("update_fields")),
                     "l2": "working set %.0f MB > L2 (126 MB): no flush needed" % (cells * bpl / 1e6),
                     "parallelism": f"replicas x{dist.world}"}
+    if mhd:
+        workload_cfg["start"] = ("finite plasma: electron gas at a background density, plasma units "
+                                 "(workloads.mhd_plasma)" if a.start == "plasma" else
+                                 "reference: electron gas empty, fields NaN within a few steps")
     metric = "D3Q19-MHD MLUPs/s" if mhd else "D3Q19 MLUPs/s"
     dtype = {"FP32": "f32", "FP16S": "f32 (FP16S storage)", "FP16C": "f32 (FP16C storage)"}[a.float_type]
 
@@ -428,9 +521,15 @@ def main():
         if dist.rank != 0:
             dist.close()
             return
-        mlups, sample, kind, cores = cpu_run(cpu_sample_cases(a, cases), max(a.steps, 1), a.ref_seconds, None)
-        line = {"metric": metric, "value": mlups, "unit": "MLUPs/s", "n_gpus": a.gpus, "steps": a.steps,
-                "warmup": a.warmup, "ms_per_step": cells / mlups / 1e3, "higher_is_better": True, "scaling": "weak",
+        # all K steps when they fit the reference arm's budget (--ref-seconds, at least 240 s here), else as
+        # many as fit; the line states the steps and warm-up steps actually run
+        ccases = cpu_sample_cases(a, cases)
+        mlups, sample, kind, cores, timed, warm = cpu_run(ccases, max(a.steps, 1), max(a.ref_seconds, 240.0), None,
+                                                          warmup=min(a.warmup, 1))
+        ccells = sum(c["config"]["n_x"] * c["config"]["n_y"] * c["config"]["n_z"] for c in ccases) / len(ccases)
+        line = {"metric": metric, "value": mlups, "unit": "MLUPs/s", "n_gpus": a.gpus, "steps": timed,
+                "steps_requested": a.steps, "warmup": warm, "warmup_requested": a.warmup,
+                "ms_per_step": ccells / mlups / 1e3, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": workload_cfg,
                 "impl": "reference",
                 "cpu_baseline": {"value": mlups, "unit": "MLUPs/s", "cores": cores, "kind": kind, "sample": sample},
@@ -601,6 +700,12 @@ def main():
         except Exception as ex:  # reported as missing rather than faked
             e2e = {"value": None, "unit": "MLUPs/s", "error": str(ex)[:200]}
     clk = clocks.stop()
+    if (a.workload == "mhd128" and not a.no_surrogate_record and dist.rank == 0 and batch is None
+            and a.field_mode != "surrogate"):
+        try:
+            extra["surrogate"] = surrogate_record(a)
+        except Exception as ex:  # reported as missing rather than faked
+            extra["surrogate"] = {"error": str(ex)[:300]}
 
     cpu = None
     if dist.rank == 0 and not a.no_cpu_baseline:
@@ -614,7 +719,7 @@ def main():
                 W.apply_case(d, c)
                 init.append({"b_stat": d.read("b_stat"), "flags": d.read("flags")})
                 d.close()
-        mlups, sample, kind, cores = cpu_run(ccases, 10 ** 6, a.ref_seconds, init)
+        mlups, sample, kind, cores, _, _ = cpu_run(ccases, 10 ** 6, a.ref_seconds, init)
         cpu = {"value": mlups, "unit": "MLUPs/s", "cores": cores, "kind": kind, "sample": sample}
 
     if dist.rank == 0:

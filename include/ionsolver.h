@@ -169,6 +169,15 @@ int ion_lbm_get_config(const ion_lbm* h, ion_config* out);
 /* ---- step loop -------------------------------------------------------- */
 /* Lbm::initialize, src/lbm/mod.rs:214-231 */
 int ion_lbm_initialize(ion_lbm* h);
+/* Finite-plasma start (no reference counterpart; MHD handles only): the next
+ * ion_lbm_initialize starts the electron gas at density rho_e0 instead of 0
+ * (src/kernels/sim_kernels.cl:823) and the charge lattice at Q + rho_e0
+ * instead of Q (sim_kernels.cl:818), so the net charge Q = rho_q - rho_e is
+ * unchanged.  The reference's electron gas starts empty, and its velocity
+ * j/rho_e turns 0/0 within a few steps (sim_kernels.cl:230-232), after which
+ * every MHD field is NaN; a background keeps the state finite.  rho_e0 = 0
+ * (the default) is the reference's start. */
+int ion_lbm_set_electron_background(ion_lbm* h, float rho_e0);
 /* Lbm::do_time_step, src/lbm/mod.rs:250-272 (asynchronous on the handle's
  * stream; the reference blocks in finish_queues, mod.rs:267-270) */
 int ion_lbm_do_time_step(ion_lbm* h);
@@ -223,7 +232,11 @@ int ion_lbm_precompute_e(ion_lbm* h);
 int ion_lbm_precompute_e_ecr(ion_lbm* h);
 
 /* ---- FP64 domain reductions (no reference counterpart) ----------------- */
-/* sum of rho and of Q over non-solid cells, accumulated in double */
+/* Total mass and total charge in double: the sums of every stored DDF slot of
+ * the gas lattice (mass) and of the charge lattice minus the electron gas
+ * (charge), decoded from their storage type and accumulated in FP64, plus the
+ * DDF shift (1 per cell and lattice).  Every slot counts, solid cells'
+ * included: what streams into a wall slot comes back out of it. */
 int ion_lbm_mass_charge(ion_lbm* h, double* mass, double* charge);
 
 /* ---- persistence (file::write / file::read, src/file.rs:12-30, 42-306;
@@ -266,7 +279,7 @@ int ion_lbm_restore(const char* path, ion_config* cfg, ion_lbm** out);
 
 /* ---- learned far field (no reference counterpart; it stands in for the far
  *      part of update_e_b_dynamic, src/kernels/sim_kernels.cl:940-955).
- *      Per cell, LOD bins within Chebyshev distance 2 of the cell's own bin
+ *      Per cell, LOD bins within Chebyshev distance 1 of the cell's own bin
  *      are summed exactly; the rest comes from a linear 3-D convolutional
  *      network on the LOD grid (4 channels in: q, q*v; 168 out: E and B at
  *      3 x 3 x 3 nodes of every block, 162 used), interpolated
@@ -339,7 +352,9 @@ int ion_batch_event_elapsed(ion_batch* b, int start, int end, float* ms);
  * first call on a device looks the array up with that device current; make
  * it before any stream capture.  All calls on a device share the array, so
  * calls that overlap on the GPU race; each call rewrites every partial it
- * reads, so nothing needs clearing between calls. */
+ * reads, so nothing needs clearing between calls.  The looked-up address is
+ * kept until the process exits: after cudaDeviceReset on a device, calls on
+ * that device are not supported. */
 #define ION_NOALLOC_MAX_VALUES 268435456ull
 int ion_ddf_sum_f64_noalloc(const void* d_values, int float_type, uint64_t count, double* d_sum, void* stream);
 

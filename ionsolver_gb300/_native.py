@@ -66,6 +66,7 @@ _SIGS = {
     "ion_lbm_destroy": (C.c_int, [_P]),
     "ion_lbm_get_config": (C.c_int, [_P, C.POINTER(Config)]),
     "ion_lbm_initialize": (C.c_int, [_P]),
+    "ion_lbm_set_electron_background": (C.c_int, [_P, C.c_float]),
     "ion_lbm_do_time_step": (C.c_int, [_P]),
     "ion_lbm_run": (C.c_int, [_P, C.c_uint64]),
     "ion_lbm_get_time_step": (C.c_int, [_P, C.POINTER(C.c_uint64)]),

@@ -113,8 +113,10 @@ int validate(const ion_config& c) {
     if (c.relaxation_time != ION_SRT && c.relaxation_time != ION_TRT) return fail(ION_E_CONFIG, "unknown relaxation_time");
     if (c.float_type < ION_FP16S || c.float_type > ION_FP32) return fail(ION_E_CONFIG, "unknown float_type");
     if (c.n_x == 0 || c.n_y == 0 || c.n_z == 0) return fail(ION_E_CONFIG, "grid sizes must be >= 1");
-    const uint64_t n = (uint64_t)c.n_x * c.n_y * c.n_z;
-    if (n >= (1ull << 32)) return fail(ION_E_CONFIG, "more than 2^32-1 cells (the reference indexes cells with uint)");
+    // n_x * n_y fits in 64 bits; checked before the third factor so the product cannot wrap
+    const uint64_t nxy = (uint64_t)c.n_x * c.n_y;
+    if (nxy >= (1ull << 32) || nxy * c.n_z >= (1ull << 32))
+        return fail(ION_E_CONFIG, "more than 2^32-1 cells (the reference indexes cells with uint)");
     if (c.velocity_set == ION_D2Q9 && c.n_z != 1) return fail(ION_E_CONFIG, "D2Q9 needs n_z == 1");
     if (c.ext_subgrid_ecr && !c.ext_magneto_hydro)
         return fail(ION_E_CONFIG, "ext_subgrid_ecr needs ext_magneto_hydro (as in the reference, mod.rs:79-80)");
@@ -533,6 +535,8 @@ int ion_lbm_create(const ion_config* cfg, ion_lbm** out) {
     g_launches++;
     L.w = h->k.w; L.ke = h->k.ke; L.kmu = h->k.kmu; L.kmu0 = h->k.kmu0; L.kkge = h->k.kkge; L.wq = h->k.wq;
     L.kkbme = h->k.kkbme; L.keabs = h->k.keabs;
+    L.rho_e0 = 0.0f;
+    L.wait_limit = WAIT_LIMIT;
     L.fx = cfg->f_x; L.fy = cfg->f_y; L.fz = cfg->f_z;
     L.ext_eq = cfg->ext_equilibrium_boundaries; L.ext_vf = cfg->ext_volume_force; L.ext_ff = cfg->ext_force_field;
     L.ext_mhd = mhd; L.update_fields = cfg->update_fields; L.trt = cfg->relaxation_time == ION_TRT;
@@ -591,6 +595,14 @@ int ion_lbm_initialize(ion_lbm* h) {
     }
     h->t = 0;
     h->initialized = true;
+    return ION_OK;
+}
+
+int ion_lbm_set_electron_background(ion_lbm* h, float rho_e0) {
+    if (!h) return fail(ION_E_INVALID, "null handle");
+    if (!h->cfg.ext_magneto_hydro) return fail(ION_E_STATE, "the electron background applies to ext_magneto_hydro");
+    if (!(rho_e0 >= 0.0f) || !std::isfinite(rho_e0)) return fail(ION_E_INVALID, "rho_e0 must be finite and >= 0");
+    h->L.rho_e0 = rho_e0;
     return ION_OK;
 }
 
@@ -987,6 +999,8 @@ int ion_lbm_load(const char* path, ion_config* cfg, ion_lbm** out) {
     c.ext_magneto_hydro = (ext & 8) != 0;
     c.mhd_lod_depth = r.u8();
     if (!r.ok) return fail(ION_E_FORMAT, "file truncated in the config block");
+    int vrc = validate(c);  // before the body size is formed from the dimensions
+    if (vrc) return vrc;
     const uint64_t N = (uint64_t)c.n_x * c.n_y * c.n_z;
     const uint64_t body = N * 17 + (c.ext_magneto_hydro ? 4 * N : 0);
     if (buf.size() - r.pos < body) return fail(ION_E_FORMAT, "Not all data could be read, file may be corrupted.");
@@ -1079,7 +1093,9 @@ int ion_lbm_restore(const char* path, ion_config* cfg, ion_lbm** out) {
     const uint32_t nx = hr.u32(), ny = hr.u32(), nz = hr.u32();
     hr.pos = 16 + 62 - 2;
     const bool mhd = (hr.u8() & 8) != 0;
-    const uint64_t N = (uint64_t)nx * ny * nz;
+    const uint64_t nxy = (uint64_t)nx * ny;
+    if (nxy >= (1ull << 32) || nxy * nz >= (1ull << 32)) return fail(ION_E_FORMAT, "grid of 2^32 or more cells");
+    const uint64_t N = nxy * nz;
     const uint64_t ext_at = 16 + 62 + N * 17 + (mhd ? 4 * N : 0);
     if (!hr.ok || ext_at + 4 > buf.size() || memcmp(buf.data() + ext_at, "IONX", 4) != 0)
         return fail(ION_E_FORMAT, "\"%s\" is not a checkpoint (no extension block)", path);

@@ -235,6 +235,8 @@ struct DevLbm {
     void* eti;             // [7][N] SUBGRID_ECR electron-temperature DDFs (or null)
     float* et;             // [N]    SUBGRID_ECR electron temperature (or null)
     float kkbme, keabs;    // DEF_KKBME, DEF_KEABS
+    float rho_e0;          // background electron density of the finite-plasma start (0: reference start)
+    uint32_t wait_limit;   // polls before a bounded wait gives up (WAIT_LIMIT unless lowered)
     uint8_t ext_eq, ext_vf, ext_ff, ext_mhd, update_fields, trt;
 };
 

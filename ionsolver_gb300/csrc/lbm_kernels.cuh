@@ -739,7 +739,11 @@ __global__ void __launch_bounds__(256) k_initialize(const DevLbm L) {
         ep_store<D, Q>((T*)L.fi, N, n, true, j, feq);
         if constexpr (MHD) {
             float aeq[7];
-            adv_equilibrium(L.q[n], ux, uy, uz, aeq);
+            // rho_e0 > 0 (finite-plasma start, no reference counterpart): ions at
+            // Q + rho_e0 and electrons at rho_e0, the same net charge Q; rho_e0 = 0 is
+            // the reference's start (electron gas at density 0, sim_kernels.cl:823)
+            const float rq0 = L.rho_e0 != 0.0f ? L.q[n] + L.rho_e0 : L.q[n];
+            adv_equilibrium(rq0, ux, uy, uz, aeq);
             const Nb7 j7{nb};
             ep_store<D, 7>((T*)L.fqi, N, n, true, j7, aeq);
 #pragma unroll
@@ -747,7 +751,7 @@ __global__ void __launch_bounds__(256) k_initialize(const DevLbm L) {
                 L.b_dyn[(size_t)c * N + n] = L.b_stat[(size_t)c * N + n];
                 L.e_dyn[(size_t)c * N + n] = L.e_stat[(size_t)c * N + n];
             }
-            equilibrium<V>(0.0f, ux, uy, uz, feq);
+            equilibrium<V>(L.rho_e0, ux, uy, uz, feq);
             ep_store<D, Q>((T*)L.ei, N, n, true, j, feq);
             if constexpr (ECR) {  // electron temperature DDFs (sim_kernels.cl:827-831)
                 adv_equilibrium(L.et[n], ux, uy, uz, aeq);

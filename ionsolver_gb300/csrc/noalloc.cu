@@ -17,11 +17,15 @@
 //     and give wrong sums; order them on one stream or synchronise;
 //   - each call overwrites exactly the partials it later reads, so nothing
 //     carries over from the previous call;
+//   - the looked-up address is kept for the life of the process: after
+//     cudaDeviceReset (or any other teardown of the device's primary context)
+//     it is stale, and calls on that device are not supported any more;
 //   - at most ION_NOALLOC_MAX_VALUES values per call (ION_E_INVALID beyond).
 #include <mutex>
 
 #include "ion_device.cuh"
 #include "ion_launch.h"
+#include "reduce_f64.cuh"
 
 namespace ion {
 
@@ -29,36 +33,6 @@ namespace ion {
 constexpr uint32_t NOALLOC_PARTS = 4096;
 constexpr uint64_t NOALLOC_PER_PART = 1ull << 16;
 static __device__ __align__(256) double g_noalloc_partials[NOALLOC_PARTS];
-
-template <int FT>
-__global__ void __launch_bounds__(RED_BLOCK) k_noalloc_partial(const void* x, uint64_t count, double* partials) {
-    __shared__ double sh[RED_BLOCK];
-    const uint64_t b = (uint64_t)blockIdx.x * NOALLOC_PER_PART;
-    const uint64_t e = min(b + NOALLOC_PER_PART, count);
-    double s = 0.0;
-    for (uint64_t i = b + threadIdx.x; i < e; i += RED_BLOCK)
-        s += (double)Ddf<FT>::ld((const typename Ddf<FT>::T*)x, i);
-    sh[threadIdx.x] = s;
-    __syncthreads();
-    for (uint32_t off = RED_BLOCK / 2; off > 0; off >>= 1) {
-        if (threadIdx.x < off) sh[threadIdx.x] += sh[threadIdx.x + off];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) partials[blockIdx.x] = sh[0];
-}
-
-__global__ void __launch_bounds__(RED_BLOCK) k_noalloc_final(const double* partials, uint32_t nparts, double* out) {
-    __shared__ double sh[RED_BLOCK];
-    double s = 0.0;
-    for (uint32_t i = threadIdx.x; i < nparts; i += RED_BLOCK) s += partials[i];
-    sh[threadIdx.x] = s;
-    __syncthreads();
-    for (uint32_t off = RED_BLOCK / 2; off > 0; off >>= 1) {
-        if (threadIdx.x < off) sh[threadIdx.x] += sh[threadIdx.x + off];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *out = sh[0];
-}
 
 // device address of g_noalloc_partials, looked up once per device
 static double* scratch_for_current_device(cudaError_t* err) {
@@ -93,11 +67,8 @@ extern "C" int ion_ddf_sum_f64_noalloc(const void* d_values, int float_type, uin
     double* partials = scratch_for_current_device(&e);
     if (!partials) return api_fail(ION_E_CUDA, cudaGetErrorString(e));
     const uint32_t nparts = (uint32_t)((count + NOALLOC_PER_PART - 1) / NOALLOC_PER_PART);
-    cudaStream_t s = (cudaStream_t)stream;
-    if (float_type == ION_FP32) k_noalloc_partial<ION_FP32><<<nparts, RED_BLOCK, 0, s>>>(d_values, count, partials);
-    else if (float_type == ION_FP16S) k_noalloc_partial<ION_FP16S><<<nparts, RED_BLOCK, 0, s>>>(d_values, count, partials);
-    else k_noalloc_partial<ION_FP16C><<<nparts, RED_BLOCK, 0, s>>>(d_values, count, partials);
-    k_noalloc_final<<<1, RED_BLOCK, 0, s>>>(partials, nparts, d_sum);
+    // the shared two-pass sum (reduce_f64.cuh) with blocks of NOALLOC_PER_PART values
+    launch_sum_two_pass(d_values, float_type, count, NOALLOC_PER_PART, nparts, partials, d_sum, (cudaStream_t)stream);
     api_count_launches(2);
     e = cudaGetLastError();
     if (e != cudaSuccess) return api_fail(ION_E_CUDA, cudaGetErrorString(e));

@@ -12,6 +12,7 @@
 //   FP64 sums : deterministic two-pass tree reductions of decoded DDFs.
 #include "ion_device.cuh"
 #include "ion_launch.h"
+#include "reduce_f64.cuh"
 
 namespace ion {
 
@@ -255,50 +256,10 @@ void launch_static_e(const DevLbm& L, const uint32_t* list, const uint32_t* coun
     k_static_e<<<grid_for(L.n, 256), 256, 0, s>>>(L, list, count, E);
 }
 
-// ---------------------------------------------------------------------------
-// FP64 sums of decoded values: fixed partition into blocks, fixed tree order
-// within a block, partials summed in block order by one thread block.
-// ---------------------------------------------------------------------------
-template <int FT>
-__device__ __forceinline__ double decode_at(const void* p, uint64_t i) {
-    return (double)Ddf<FT>::ld((const typename Ddf<FT>::T*)p, i);
-}
-
-template <int FT>
-__global__ void __launch_bounds__(RED_BLOCK) k_sum_partial(const void* x, uint64_t count, double* partials) {
-    __shared__ double sh[RED_BLOCK];
-    const uint64_t per = (count + gridDim.x - 1) / gridDim.x;
-    const uint64_t b = (uint64_t)blockIdx.x * per, e = min(b + per, count);
-    double s = 0.0;
-    for (uint64_t i = b + threadIdx.x; i < e; i += RED_BLOCK) s += decode_at<FT>(x, i);
-    sh[threadIdx.x] = s;
-    __syncthreads();
-    for (uint32_t off = RED_BLOCK / 2; off > 0; off >>= 1) {
-        if (threadIdx.x < off) sh[threadIdx.x] += sh[threadIdx.x + off];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) partials[blockIdx.x] = sh[0];
-}
-
-__global__ void __launch_bounds__(RED_BLOCK) k_sum_final(const double* partials, uint32_t nparts, double* out) {
-    __shared__ double sh[RED_BLOCK];
-    double s = 0.0;
-    for (uint32_t i = threadIdx.x; i < nparts; i += RED_BLOCK) s += partials[i];
-    sh[threadIdx.x] = s;
-    __syncthreads();
-    for (uint32_t off = RED_BLOCK / 2; off > 0; off >>= 1) {
-        if (threadIdx.x < off) sh[threadIdx.x] += sh[threadIdx.x + off];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *out = sh[0];
-}
-
 void launch_sum_f64(const void* x, int ft, uint64_t count, double* partials, uint32_t nparts, double* out,
                     cudaStream_t s) {
-    if (ft == ION_FP32) k_sum_partial<ION_FP32><<<nparts, RED_BLOCK, 0, s>>>(x, count, partials);
-    else if (ft == ION_FP16S) k_sum_partial<ION_FP16S><<<nparts, RED_BLOCK, 0, s>>>(x, count, partials);
-    else k_sum_partial<ION_FP16C><<<nparts, RED_BLOCK, 0, s>>>(x, count, partials);
-    k_sum_final<<<1, RED_BLOCK, 0, s>>>(partials, nparts, out);
+    // nparts blocks of ceil(count / nparts) values (reduce_f64.cuh)
+    launch_sum_two_pass(x, ft, count, (count + nparts - 1) / nparts, nparts, partials, out, s);
 }
 
 // ---------------------------------------------------------------------------

@@ -215,6 +215,11 @@ class Lbm:
     def initialize(self) -> None:
         N.check(N.lib().ion_lbm_initialize(self._h))
 
+    def set_electron_background(self, rho_e0: float) -> None:
+        """Finite-plasma start of the next initialize (no reference counterpart):
+        electron gas at density rho_e0, charge lattice at Q + rho_e0."""
+        N.check(N.lib().ion_lbm_set_electron_background(self._h, float(rho_e0)))
+
     def do_time_step(self) -> None:
         N.check(N.lib().ion_lbm_do_time_step(self._h))
 

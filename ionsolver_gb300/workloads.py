@@ -7,8 +7,12 @@
   component (seed 2), rho = 1, an axially magnetised disk magnet centred on
   the z = 1 face, Units{m=1, kg=1, s=1, a=1e-6}, LOD depth 4.
 
+* ``mhd_plasma``: ``mhd_box`` with the finite-plasma start (a background
+  electron density; units in which the electron response per step is small).
+
 A case is a dict ``{"config": {...C field names...}, "fields": {...},
-"meshes": [(p0, p1, p2, model, values)], "precompute_b": bool}`` that
+"meshes": [(p0, p1, p2, model, values)], "precompute_b": bool}`` (optionally
+``"electron_background": rho_e0``) that
 ``apply_case`` writes into any object with ``write``/``add_mesh``/
 ``voxelise_mesh``/``precompute_B`` (the GPU ``Lbm``; tests adapt the CPU
 oracle to the same calls).
@@ -22,6 +26,19 @@ from .meshes import annulus, cylinder
 
 NU_1_30 = float(np.float32(1.0) / np.float32(30.0))  # tau = 0.6
 MAGNETIZATION_SI = 8.0e10  # A/m: gives max |B_stat| of a few 1e-2 lattice units with a = 1e-6
+
+# The finite-plasma start.  The reference's electron gas starts at density 0
+# (sim_kernels.cl:823) and its velocity j/rho_e turns 0/0 within a few steps;
+# from then on every MHD field is NaN.  With a background electron density
+# rho_e0 the state stays finite if the units keep the electron response per
+# step small: electron acceleration per unit net charge KE/(2|KKGE|) ~ 3e-3,
+# cyclotron rotation B/(2|KKGE|) ~ 1e-2 per step and plasma frequency
+# sqrt(4 pi KE rho_e0/|KKGE|) ~ 0.03 per step.  Units: cells of 6.46 cm,
+# steps of 1 ns, gas 1e-3 kg/m^3 (kg = 1e-3 m^3), current unit 1 A; every
+# intermediate of the float32 unit conversion stays a normal float.
+PLASMA_UNITS = dict(m=0.0646, kg=2.7e-7, s=1e-9, a=1.0, k=1.0, prop=0)
+PLASMA_MAGNETIZATION_SI = 300.0  # A/m: max |B_stat| ~ 1e-2 |2 KKGE| in these units
+PLASMA_RHO_E0 = 0.01             # background electron density (lattice charge units)
 
 
 def taylor_green(n: int = 64, amplitude: float = 0.05, float_type: int = 2, relaxation_time: int = 0,
@@ -73,6 +90,38 @@ def mhd_box(n: int = 128, float_type: int = 2, depth: int = 4, field_mode: int =
     }
 
 
+def to_plasma(case: dict, rho_e0: float = PLASMA_RHO_E0) -> dict:
+    """A case of ``mhd_box`` switched to the finite-plasma start: PLASMA_UNITS,
+    every magnet at PLASMA_MAGNETIZATION_SI (same direction), the electron gas
+    starting at rho_e0.  Fields, geometry and seeds are unchanged."""
+    case["config"]["units"] = dict(PLASMA_UNITS)
+    meshes = []
+    for p0, p1, p2, model, vals in case["meshes"]:
+        if model == "magnet":
+            m = np.asarray(vals, np.float64)
+            vals = tuple(float(v) for v in m / np.linalg.norm(m) * PLASMA_MAGNETIZATION_SI)
+        meshes.append((p0, p1, p2, model, vals))
+    case["meshes"] = meshes
+    case["electron_background"] = float(rho_e0)
+    return case
+
+
+def mhd_plasma(n: int = 128, float_type: int = 2, depth: int = 4, field_mode: int = 0, magnet_r: float | None = None,
+               magnet_t: float | None = None, shape: tuple | None = None, update_fields: int = 1,
+               rho_e0: float = PLASMA_RHO_E0, rings: bool = False) -> dict:
+    """``mhd_box`` with the finite-plasma start: the same seeded charge and
+    velocity fields, wall shell and disk magnet (radius n/8, thickness n/16
+    unless given: 16 and 8 cells at 128^3; or the two rings), in PLASMA_UNITS
+    with the magnets at PLASMA_MAGNETIZATION_SI and the electron gas starting
+    at rho_e0."""
+    nx = (shape or (n, n, n))[0]
+    case = mhd_box(n=n, float_type=float_type, depth=depth, field_mode=field_mode,
+                   magnet_r=magnet_r if magnet_r is not None else nx / 8.0,
+                   magnet_t=magnet_t if magnet_t is not None else nx / 16.0, shape=shape,
+                   update_fields=update_fields, rings=rings)
+    return to_plasma(case, rho_e0)
+
+
 def ecr_box(n: int = 32, float_type: int = 2, depth: int = 2, relaxation_time: int = 0, seed_t: int = 9) -> dict:
     """The SUBGRID_ECR extension on an MHD box: a disk magnet, two ChargedECR plates
     (+/- 1e-13 C per cell, 1/4 and 3/4 of the box in y) for the oscillating field
@@ -94,7 +143,7 @@ def ecr_box(n: int = 32, float_type: int = 2, depth: int = 2, relaxation_time: i
 
 
 def batch_domains(count: int = 96, float_type: int = 2, field_mode: int = 1, seed_sizes: int = 3,
-                  seed_magnets: int = 4) -> list[dict]:
+                  seed_magnets: int = 4, plasma: bool = False) -> list[dict]:
     """Uneven MHD domains: cube edges uniform from {32,48,64,80,96} (PCG64
     seed 3); a disk magnet per domain with radius uniform in {4..12} cells,
     thickness r/2, at a random centre that keeps it inside the walls (seed 4);
@@ -113,7 +162,7 @@ def batch_domains(count: int = 96, float_type: int = 2, field_mode: int = 1, see
         p0, p1, p2 = cylinder(c, r, t, axis=2)
         case["meshes"] = [(p0, p1, p2, "magnet", (0.0, 0.0, MAGNETIZATION_SI))]
         case["precompute_b"] = True
-        cases.append(case)
+        cases.append(to_plasma(case) if plasma else case)
     return cases
 
 
@@ -138,6 +187,8 @@ def apply_case(lbm, case: dict) -> None:
     from .lbm import ModelType
     for name, arr in case["fields"].items():
         lbm.write(name, arr)
+    if case.get("electron_background"):
+        lbm.set_electron_background(case["electron_background"])
     for p0, p1, p2, model, vals in case["meshes"]:
         idx = lbm.add_mesh(p0, p1, p2)
         lbm.voxelise_mesh(idx, ModelType(MODEL_IDS[model], tuple(vals)))

@@ -106,6 +106,8 @@ def _bind(lib: C.CDLL) -> C.CDLL:
     lib.orc_set_threads.argtypes = [C.c_int]
     if hasattr(lib, "orc_set_nan_model"):
         lib.orc_set_nan_model.argtypes = [C.c_int]
+    if hasattr(lib, "orc_set_electron_background"):
+        lib.orc_set_electron_background.argtypes = [C.c_void_p, C.c_float]
     fp = C.POINTER(C.c_float)
     lib.orc_voxelize.restype = C.c_int
     lib.orc_voxelize.argtypes = [C.c_void_p, fp, fp, fp, C.c_uint32, fp, fp, C.c_int, C.c_float, C.c_float,
@@ -218,6 +220,10 @@ class OracleLbm:
         a = self.field(name)
         v = np.asarray(values).reshape(-1)
         a[: v.size] = v.astype(a.dtype)
+
+    def set_electron_background(self, rho_e0: float) -> None:
+        """The finite-plasma start of the next initialize (restatement only)."""
+        self.lib.orc_set_electron_background(self.h, float(rho_e0))
 
     def initialize(self):
         self._threads()

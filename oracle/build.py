@@ -14,7 +14,8 @@ Two CPU oracles are built here:
   runtime values here.
 
 The kernel text is taken from the reference checkout (``ION_REFERENCE_ROOT``,
-default ``/root/reference``) as ``src/opencl.rs:67-75`` does: everything after
+or ``--reference PATH`` when this file runs as a script) as
+``src/opencl.rs:67-75`` does: everything after
 the ``EndTempDefines%`` marker.  Two mechanical rewrites make it C++:
 OpenCL vector literals ``(float3)(a,b,c)`` become constructor calls, and the
 voxeliser's ``distances`` array gets one guard element in front (its
@@ -44,8 +45,11 @@ CC = os.environ.get("CC", "gcc")
 COMMON_FLAGS = ["-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fwrapv", "-fno-fast-math"]
 
 
-def reference_root() -> Path:
-    return Path(os.environ.get("ION_REFERENCE_ROOT", "/root/reference"))
+def reference_root() -> Path | None:
+    """The IonSolver checkout: ION_REFERENCE_ROOT, or ``--reference PATH`` on this
+    script's command line (which sets it).  None when neither is given."""
+    root = os.environ.get("ION_REFERENCE_ROOT")
+    return Path(root) if root else None
 
 
 def _run(cmd: list[str]) -> None:
@@ -81,8 +85,9 @@ def generate_reference_body() -> bool:
 
     Returns False when neither the checkout nor a previously generated body
     is available (the reference oracle is then unavailable)."""
-    cl = reference_root() / "src" / "kernels" / "sim_kernels.cl"
-    if not cl.exists():
+    root = reference_root()
+    cl = root / "src" / "kernels" / "sim_kernels.cl" if root else None
+    if cl is None or not cl.exists():
         return BODY.exists()
     text = cl.read_text()
     parts = text.split("EndTempDefines%")
@@ -205,6 +210,8 @@ def build_reference(cfg: dict) -> Path | None:
 
 
 def main() -> int:
+    if "--reference" in sys.argv:
+        os.environ["ION_REFERENCE_ROOT"] = sys.argv[sys.argv.index("--reference") + 1]
     print(build_oracle(force="--force" in sys.argv))
     print("reference kernels available:", reference_available())
     return 0

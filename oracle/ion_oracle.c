@@ -162,6 +162,9 @@ typedef struct {
     /* per-cell LOD contributions of the current step */
     R* lodc;
     uint8_t* lodm;
+    /* background electron density of the finite-plasma start (0: the
+     * reference's start, electron gas at density 0) */
+    R rho_e0;
 } orc;
 
 static int g_threads = 1;
@@ -722,6 +725,13 @@ void* orc_field(void* p, int field, size_t* elem_bytes, size_t* count) {
 
 uint64_t orc_time_step(void* p) { return ((orc*)p)->t; }
 
+/* The finite-plasma start (no reference counterpart, applied by the next
+ * initialize): the electron gas starts at density rho_e0 instead of 0
+ * (sim_kernels.cl:823) and the charge lattice at Q + rho_e0 instead of Q
+ * (sim_kernels.cl:818), so the net charge Q is unchanged.  With rho_e0 = 0
+ * initialize is the reference's. */
+void orc_set_electron_background(void* p, float rho_e0) { ((orc*)p)->rho_e0 = (R)rho_e0; }
+
 /* initialize kernel (sim_kernels.cl:760-832) + Lbm::initialize (mod.rs:214-231) */
 void orc_initialize(void* p) {
     orc* h = (orc*)p;
@@ -744,11 +754,13 @@ void orc_initialize(void* p) {
         if (mhd) {
             R aeq[7];
             uint64_t j7[7];
-            adv_equilibrium(h->qf[n], h->u[n], h->u[N + n], h->u[2 * N + n], aeq);
+            /* finite-plasma start: ions at Q + rho_e0, electrons at rho_e0 */
+            const R rhoq0 = h->rho_e0 != (R)0 ? h->qf[n] + h->rho_e0 : h->qf[n];
+            adv_equilibrium(rhoq0, h->u[n], h->u[N + n], h->u[2 * N + n], aeq);
             neighbours7(h, n, j7);
             ep_store(h, h->fqi, 7, n, j7, 1, aeq);
             for (int c = 0; c < 3; c++) { h->b_dyn[c * N + n] = h->b_stat[c * N + n]; h->e_dyn[c * N + n] = h->e_stat[c * N + n]; }
-            equilibrium(h, (R)0, h->u[n], h->u[N + n], h->u[2 * N + n], feq);
+            equilibrium(h, h->rho_e0, h->u[n], h->u[N + n], h->u[2 * N + n], feq);
             ep_store(h, h->ei, q, n, j, 1, feq);
             if (h->eti) { /* electron temperature DDFs (827-831) */
                 adv_equilibrium(h->et[n], h->u[n], h->u[N + n], h->u[2 * N + n], aeq);

@@ -19,6 +19,8 @@ def setup_oracle(case, kind="f32", threads=None, canonical_nan=False):
     o._threads()
     for name, arr in case["fields"].items():
         o.set_field(name, arr)
+    if case.get("electron_background") and kind != "ref":  # "ref": see initialize_oracle
+        o.set_electron_background(case["electron_background"])
     for p0, p1, p2, model, vals in case["meshes"]:
         o.voxelise(p0, p1, p2, model, vals)
     if case["precompute_b"]:
@@ -30,9 +32,24 @@ def setup_oracle(case, kind="f32", threads=None, canonical_nan=False):
     return o
 
 
+def initialize_oracle(o, case):
+    """initialize, plus the finite-plasma start where the case asks for it.  The
+    reference's kernels have no such start (their electron gas starts at 0), so
+    for them the electron and charge DDFs after initialize are taken from the
+    restatement's initialize: the same calculate_f_eq / calculate_a_eq, at
+    density rho_e0 and Q + rho_e0."""
+    o.initialize()
+    if case.get("electron_background") and o.kind == "ref":
+        r = setup_oracle(case, "f32", o.threads, o.canonical_nan)
+        r.initialize()
+        for name in ("ei", "fqi"):
+            o.set_field(name, r.field(name))
+        r.close()
+
+
 def run_oracle(case, steps, kind="f32", threads=None, canonical_nan=False):
     o = setup_oracle(case, kind, threads, canonical_nan)
-    o.initialize()
+    initialize_oracle(o, case)
     o.run(steps)
     return o
 

@@ -44,6 +44,11 @@ def geometry():
     return case
 
 
+def plasma(ft, n, depth):
+    """The finite-plasma start (electron background, plasma units)."""
+    return W.mhd_plasma(n=n, float_type=ft, depth=depth, magnet_r=n / 4, magnet_t=n / 5)
+
+
 def ecr(ft, rt):
     return W.ecr_box(n=16, float_type=ft, depth=2, relaxation_time=rt)
 
@@ -58,6 +63,8 @@ CASES = {
     "mhd16_fp32_d2": (lambda: mhd(2, 16, 2), 6, "run"),
     "mhd16_fp16s_d2": (lambda: mhd(0, 16, 2), 6, "run"),
     "mhd16_fp32_d4": (lambda: mhd(2, 16, 4), 4, "run"),
+    "plasma16_fp32_d2": (lambda: plasma(2, 16, 2), 30, "run"),
+    "plasma16_fp16c_d2": (lambda: plasma(1, 16, 2), 30, "run"),
     "geometry": (geometry, 0, "setup"),
     "ecr16_fp32_srt": (lambda: ecr(2, 0), 4, "run"),
     "ecr16_fp16s_trt": (lambda: ecr(0, 1), 3, "run"),

@@ -44,7 +44,7 @@ def run_case(name, kind, inputs=None):
     if action == "setup":
         o.precompute_e()
     else:
-        o.initialize()
+        U.initialize_oracle(o, case)
         o.run(steps)
     return case, o
 

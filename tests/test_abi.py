@@ -2,7 +2,10 @@
 include/ionsolver.h declares, and rejects bad configurations and files with
 the documented status codes before touching the device."""
 import ctypes as C
+import os
 import re
+import subprocess
+import sys
 from pathlib import Path
 
 import numpy as np
@@ -11,7 +14,8 @@ import pytest
 import ionsolver_gb300 as I
 from ionsolver_gb300 import _native as N
 
-HEADER = Path(__file__).resolve().parent.parent / "include" / "ionsolver.h"
+ROOT = Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "ionsolver.h"
 
 
 def declared_functions():
@@ -45,7 +49,10 @@ def test_abi_version_and_defaults():
     (dict(ext_magneto_hydro=1), -2), (dict(ext_magneto_hydro=1, ext_volume_force=1, n_x=20), -2),
     (dict(ext_subgrid_ecr=1), -2), (dict(n_x=0), -2), (dict(float_type=7), -2),
     (dict(ext_magneto_hydro=1, ext_volume_force=1, mhd_lod_depth=5), -2),
-    (dict(n_x=2048, n_y=2048, n_z=1024), -2), (dict(n_x=65536, n_y=65536, n_z=1), -2)])
+    (dict(n_x=2048, n_y=2048, n_z=1024), -2), (dict(n_x=65536, n_y=65536, n_z=1), -2),
+    # products that wrap past 2^64 if formed before the check: 2^31 * 2^31 * 4 = 2^64 -> 0,
+    # (2^32-1)^2 * 2^31 -> 2^31 modulo 2^64
+    (dict(n_x=2 ** 31, n_y=2 ** 31, n_z=4), -2), (dict(n_x=2 ** 32 - 1, n_y=2 ** 32 - 1, n_z=2 ** 31), -2)])
 def test_create_rejects_configs(change, code):
     c = I.LbmConfig(velocity_set=2, n_x=32, n_y=32, n_z=32, float_type=2)
     for k, v in change.items():
@@ -83,12 +90,21 @@ def test_null_arguments_are_errors():
 
 
 def test_create_without_a_device_is_an_error_not_an_abort():
-    """A valid configuration on a host without a usable CUDA device: ION_E_CUDA and a
-    message (the reference exits the process instead, opencl.rs:11-13)."""
-    torch = pytest.importorskip("torch")
-    if torch.cuda.is_available():
-        pytest.skip("a CUDA device is present")
-    c = I.LbmConfig(velocity_set=2, n_x=1024, n_y=1024, n_z=1024, float_type=2)
-    h = C.c_void_p()
-    assert N.lib().ion_lbm_create(C.byref(c.to_c()), C.byref(h)) == -3 and not h.value
-    assert b"CUDA" in N.lib().ion_last_error()
+    """A valid configuration in a process that sees no CUDA device: ION_E_CUDA and a
+    message (the reference exits the process instead, opencl.rs:11-13).  Runs in a
+    child process with CUDA_VISIBLE_DEVICES empty, so it holds on a GPU host too."""
+    code = (
+        "import ctypes as C, sys\n"
+        "sys.path.insert(0, %r)\n"
+        "import ionsolver_gb300 as I\n"
+        "from ionsolver_gb300 import _native as N\n"
+        "c = I.LbmConfig(velocity_set=2, n_x=32, n_y=32, n_z=32, float_type=2)\n"
+        "h = C.c_void_p()\n"
+        "rc = N.lib().ion_lbm_create(C.byref(c.to_c()), C.byref(h))\n"
+        "if h.value: N.lib().ion_lbm_destroy(h)\n"
+        "print(rc, N.lib().ion_last_error().decode())\n" % str(ROOT))
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    rc, msg = r.stdout.strip().split(" ", 1)
+    assert int(rc) == -3 and "CUDA" in msg

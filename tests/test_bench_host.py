@@ -30,12 +30,34 @@ def test_bytes_per_lattice_update():
 def test_workload_names(monkeypatch):
     seen = []
     monkeypatch.setattr(W, "mhd_box", lambda **kw: seen.append(kw) or {"config": {}})
-    a = types.SimpleNamespace(field_mode="surrogate", float_type="FP16S", workload="rings192d3")
+    a = types.SimpleNamespace(field_mode="surrogate", float_type="FP16S", workload="rings192d3", start="reference")
     bench.make_cases(a)
     a.workload = "rings384"
     bench.make_cases(a)
     assert (seen[0]["n"], seen[0]["depth"], seen[0]["rings"]) == (192, 3, True)
     assert (seen[1]["n"], seen[1]["depth"]) == (384, 4)
+
+
+def test_plasma_start_cases():
+    """--start plasma: the same geometry and seeds, plasma units, the electron background."""
+    a = types.SimpleNamespace(field_mode="fast", float_type="FP32", workload="mhd64", start="plasma")
+    c = bench.make_cases(a)[0]
+    r = bench.make_cases(types.SimpleNamespace(**dict(vars(a), start="reference")))[0]
+    assert c["electron_background"] == W.PLASMA_RHO_E0 and "electron_background" not in r
+    assert c["config"]["units"] == W.PLASMA_UNITS
+    for k in ("q", "u", "flags"):
+        assert np.array_equal(c["fields"][k], r["fields"][k])
+    assert np.array_equal(c["meshes"][0][0], r["meshes"][0][0])
+    assert c["meshes"][0][4] == (0.0, 0.0, W.PLASMA_MAGNETIZATION_SI)
+
+
+def test_reference_arm_reports_the_steps_it_ran(monkeypatch):
+    """A CPU sample that runs out of budget reports the steps it timed, not the steps asked for."""
+    case = W.mhd_plasma(n=16, depth=2, magnet_r=4.0, magnet_t=3.0)
+    mlups, sample, kind, cores, timed, warm = bench.cpu_run([case], 1000, 0.0, None, warmup=1)
+    assert timed == 1 and warm == 1 and mlups > 0 and "1 full timestep" in sample
+    mlups, sample, kind, cores, timed, warm = bench.cpu_run([case], 3, 1e9, None)
+    assert timed == 3 and warm == 0
 
 
 def _bins(cfg):

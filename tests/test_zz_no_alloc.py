@@ -29,7 +29,7 @@ def _noalloc_sum(lbm, d_out) -> float:
     return float(d_out.item())
 
 
-@pytest.mark.parametrize("ft", [2, 0], ids=["FP32", "FP16S"])
+@pytest.mark.parametrize("ft", [2, 0, 1], ids=["FP32", "FP16S", "FP16C"])
 def test_noalloc_sum_matches_mass_charge_on_two_calls(ft):
     case = W.taylor_green(shape=(48, 40, 32), amplitude=0.05, float_type=ft)
     case["fields"]["flags"] = W.shell_flags(48, 40, 32)
