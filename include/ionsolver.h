@@ -45,7 +45,7 @@ enum { ION_D2Q9 = 0, ION_D3Q15 = 1, ION_D3Q19 = 2, ION_D3Q27 = 3 };
 enum { ION_SRT = 0, ION_TRT = 1 };
 /* FloatType, src/lbm/types.rs:75-83 */
 enum { ION_FP16S = 0, ION_FP16C = 1, ION_FP32 = 2 };
-/* Propellant, src/lbm/units.rs:324-332 */
+/* Propellant, src/lbm/units.rs:214-222 */
 enum { ION_PROP_H = 0, ION_PROP_HE, ION_PROP_NE, ION_PROP_AR, ION_PROP_KR, ION_PROP_XE };
 /* How the dynamic E/B far field is evaluated each step (no reference
  * counterpart: the reference always runs update_e_b_dynamic,
@@ -81,7 +81,7 @@ enum {
 /* ModelType -> flag byte, src/mesh.rs:9-14, 309-314 */
 enum { ION_MODEL_SOLID = 0, ION_MODEL_MAGNET = 1, ION_MODEL_CHARGED = 2, ION_MODEL_CHARGED_ECR = 3 };
 
-/* Units, src/lbm/units.rs:122-137 */
+/* Units, src/lbm/units.rs:14-27 */
 typedef struct ion_units {
     float m, kg, s, a, k;
     int32_t prop;
@@ -112,7 +112,7 @@ typedef struct ion_config {
 } ion_config;
 
 /* Constants derived from Units that the kernels use
- * (src/lbm/units.rs:145-177, 259-307; src/lbm/domain.rs:808, 838-848). */
+ * (src/lbm/units.rs:149-197; src/lbm/domain.rs:808, 838-848). */
 typedef struct ion_constants {
     float w;        /* DEF_W   = 1/(3 nu + 1/2)            */
     float ke;       /* DEF_KE  = ke_lu                     */
@@ -147,16 +147,16 @@ uint64_t ion_kernel_launch_count(void);
 
 /* LbmConfig::new(), src/lbm/mod.rs:105-135 */
 int ion_config_default(ion_config* cfg);
-/* Units::new(), src/lbm/units.rs:140-149 */
+/* Units::new(), src/lbm/units.rs:30-39 */
 int ion_units_default(ion_units* u);
-/* Units::set(...), src/lbm/units.rs:151-169 */
+/* Units::set(...), src/lbm/units.rs:41-60 */
 int ion_units_set(ion_units* u, float lbm_length, float lbm_velocity, float lbm_rho,
                   float lbm_charge, float lbm_temp, float si_length, float si_velocity,
                   float si_rho, float si_charge, float si_temp);
 /* The kernel constants for a config (get_device_defines, src/lbm/domain.rs:736-858) */
 int ion_constants_from_config(const ion_config* cfg, ion_constants* out);
 /* Units::nu_si_lu / magnetization_si_lu / charge_si_lu / len_si_lu
- * (src/lbm/units.rs:236-257, 212-214): what selects the conversion:
+ * (src/lbm/units.rs:126-128, 145-147, 130-133, 102-104): what selects the conversion:
  * 0 = nu, 1 = magnetization, 2 = charge, 3 = length. */
 int ion_units_si_to_lu(const ion_units* u, int what, float value, float* out);
 
@@ -190,6 +190,16 @@ int ion_lbm_get_time_step(const ion_lbm* h, uint64_t* t);
  * returns ION_E_TIMEOUT if the stream is still busy after timeout_ms
  * (timeout_ms < 0: wait without bound). */
 int ion_lbm_finish_queues(ion_lbm* h, int timeout_ms);
+/* Bounded device waits (no reference counterpart; the reference's OpenCL
+ * kernels do not wait on each other).  The row-staged stream_collide and the
+ * E/B update wait for data they staged with bulk copies; a wait gives up after
+ * `polls` polls, records the failure, lets its copies in flight land and skips
+ * the rest of the launch, and ion_lbm_finish_queues then returns ION_E_TIMEOUT.
+ * Default ION_WAIT_LIMIT_DEFAULT; 0 gives up at the first wait (used to test
+ * the timeout path).  The skipped work leaves the state incomplete: initialize
+ * again after a timeout. */
+#define ION_WAIT_LIMIT_DEFAULT 16777216u
+int ion_lbm_set_wait_limit(ion_lbm* h, uint32_t polls);
 /* LbmDomain::enqueue_update_fields, src/lbm/domain.rs:432-441 */
 int ion_lbm_update_fields(ion_lbm* h);
 
@@ -218,6 +228,10 @@ int ion_lbm_import_mesh_reposition(ion_lbm* h, const char* path, float cx, float
                                    float rx, float ry, float rz, float size, uint32_t* index);
 /* Mesh::translate, src/mesh.rs:121-130 */
 int ion_lbm_mesh_translate(ion_lbm* h, uint32_t index, float dx, float dy, float dz);
+/* a mesh's vertices, [ntri][3] each (the p0/p1/p2 arrays of Mesh,
+ * src/mesh.rs:71-79); with p0 = p1 = p2 = NULL only *ntri is set */
+int ion_lbm_mesh_triangles(const ion_lbm* h, uint32_t index, float* p0, float* p1, float* p2, uint32_t capacity,
+                           uint32_t* ntri);
 /* mesh bounds: out[0..2] = p_min, out[3..5] = p_max, out[6..8] = center */
 int ion_lbm_mesh_bounds(const ion_lbm* h, uint32_t index, float* out9);
 /* Lbm::voxelise_mesh(index, ModelType), src/mesh.rs:256-343.
@@ -334,6 +348,12 @@ int ion_batch_destroy(ion_batch* b);
 int ion_batch_run(ion_batch* b, uint64_t steps);
 /* bounded wait for the batch's stream; reports device-side timeouts */
 int ion_batch_finish(ion_batch* b, int timeout_ms);
+/* the batch step's poll limits: grid barrier between its phases (default
+ * ION_BARRIER_LIMIT_DEFAULT, polls 64 ns apart) and staged-tile waits of every
+ * domain (as ion_lbm_set_wait_limit); a wait that gives up ends the launch
+ * and ion_batch_finish returns ION_E_TIMEOUT */
+#define ION_BARRIER_LIMIT_DEFAULT 67108864u
+int ion_batch_set_wait_limits(ion_batch* b, uint32_t barrier_polls, uint32_t tile_polls);
 /* autotuner record i (block, grid, ms per step); i = 0xFFFFFFFF: the chosen shape */
 int ion_batch_tuning(ion_batch* b, uint32_t i, uint32_t* block, uint32_t* grid, float* ms_per_step);
 int ion_batch_record_event(ion_batch* b, int slot);

@@ -12,6 +12,9 @@ _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "_build" / "libionsolver.so"
 
 ION_OK = 0
+ION_E_TIMEOUT = -7
+ION_WAIT_LIMIT_DEFAULT = 16777216      # include/ionsolver.h
+ION_BARRIER_LIMIT_DEFAULT = 67108864
 ERRORS = {-1: "ION_E_INVALID", -2: "ION_E_CONFIG", -3: "ION_E_CUDA", -4: "ION_E_NOMEM", -5: "ION_E_IO",
           -6: "ION_E_FORMAT", -7: "ION_E_TIMEOUT", -8: "ION_E_STATE"}
 
@@ -23,7 +26,7 @@ class IonError(RuntimeError):
 
 
 class Units(C.Structure):
-    """Units (IonSolver src/lbm/units.rs:122-137)."""
+    """Units (IonSolver src/lbm/units.rs:14-27)."""
     _fields_ = [("m", C.c_float), ("kg", C.c_float), ("s", C.c_float), ("a", C.c_float), ("k", C.c_float),
                 ("prop", C.c_int32)]
 
@@ -67,6 +70,7 @@ _SIGS = {
     "ion_lbm_get_config": (C.c_int, [_P, C.POINTER(Config)]),
     "ion_lbm_initialize": (C.c_int, [_P]),
     "ion_lbm_set_electron_background": (C.c_int, [_P, C.c_float]),
+    "ion_lbm_set_wait_limit": (C.c_int, [_P, C.c_uint32]),
     "ion_lbm_do_time_step": (C.c_int, [_P]),
     "ion_lbm_run": (C.c_int, [_P, C.c_uint64]),
     "ion_lbm_get_time_step": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
@@ -82,6 +86,7 @@ _SIGS = {
     "ion_lbm_import_mesh_reposition": (C.c_int, [_P, C.c_char_p] + [C.c_float] * 7 + [C.POINTER(C.c_uint32)]),
     "ion_lbm_mesh_translate": (C.c_int, [_P, C.c_uint32, C.c_float, C.c_float, C.c_float]),
     "ion_lbm_mesh_bounds": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_float)]),
+    "ion_lbm_mesh_triangles": (C.c_int, [_P, C.c_uint32, _P, _P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
     "ion_lbm_voxelise_mesh": (C.c_int, [_P, C.c_uint32, C.c_int, C.c_float, C.c_float, C.c_float]),
     "ion_lbm_precompute_b": (C.c_int, [_P]),
     "ion_lbm_precompute_e": (C.c_int, [_P]),
@@ -120,6 +125,7 @@ _SIGS = {
     "ion_batch_destroy": (C.c_int, [_P]),
     "ion_batch_run": (C.c_int, [_P, C.c_uint64]),
     "ion_batch_finish": (C.c_int, [_P, C.c_int]),
+    "ion_batch_set_wait_limits": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
     "ion_batch_tuning": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                    C.POINTER(C.c_float)]),
     "ion_batch_record_event": (C.c_int, [_P, C.c_int]),

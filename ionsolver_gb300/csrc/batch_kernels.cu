@@ -20,7 +20,6 @@
 
 namespace ion {
 
-constexpr uint32_t BARRIER_LIMIT = 1u << 26;
 
 __device__ __forceinline__ uint32_t find_domain(const uint32_t* off, uint32_t ndom, uint32_t idx) {
     uint32_t lo = 0, hi = ndom;  // off[lo] <= idx < off[hi]
@@ -33,8 +32,8 @@ __device__ __forceinline__ uint32_t find_domain(const uint32_t* off, uint32_t nd
 }
 
 // Generation barrier over all blocks of a co-resident grid.  Returns false
-// (block-uniform) when it gave up after BARRIER_LIMIT polls.
-__device__ __forceinline__ bool grid_barrier(uint32_t* count, uint32_t* gen, uint32_t nblocks) {
+// (block-uniform) when it gave up after `limit` polls.
+__device__ __forceinline__ bool grid_barrier(uint32_t* count, uint32_t* gen, uint32_t nblocks, uint32_t limit) {
     __syncthreads();
     int ok = 1;
     if (threadIdx.x == 0) {
@@ -47,7 +46,7 @@ __device__ __forceinline__ bool grid_barrier(uint32_t* count, uint32_t* gen, uin
         } else {
             uint32_t i = 0;
             while (*(volatile uint32_t*)gen == g) {
-                if (++i > BARRIER_LIMIT) { ok = 0; break; }
+                if (++i > limit) { ok = 0; break; }
                 __nanosleep(64);
             }
         }
@@ -85,7 +84,7 @@ __global__ void __launch_bounds__(256, 2) k_batch_step(const BatchDev B, const u
         }
     }
     if constexpr (MHD) {
-        if (!grid_barrier(B.bar_count, B.bar_gen, nblocks)) { if (threadIdx.x == 0) atomicExch(B.err, 2u); return; }
+        if (!grid_barrier(B.bar_count, B.bar_gen, nblocks, B.barrier_limit)) { if (threadIdx.x == 0) atomicExch(B.err, 2u); return; }
         // phase B: LOD bins, one warp per bin
         const uint32_t warps = nblocks * (blockDim.x >> 5);
         for (uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < B.total_bins; w += warps) {
@@ -94,7 +93,7 @@ __global__ void __launch_bounds__(256, 2) k_batch_step(const BatchDev B, const u
             if (L.depth > 0u) lod_bin_warp(L, w - B.bin_off[d], threadIdx.x & 31u);
             else if ((threadIdx.x & 31u) < 4u) L.qu_lod[threadIdx.x & 31u] = 0.0f;
         }
-        if (!grid_barrier(B.bar_count, B.bar_gen, nblocks)) { if (threadIdx.x == 0) atomicExch(B.err, 2u); return; }
+        if (!grid_barrier(B.bar_count, B.bar_gen, nblocks, B.barrier_limit)) { if (threadIdx.x == 0) atomicExch(B.err, 2u); return; }
         // phase C: E/B update
         eb_init(sm);
         uint32_t uses[2] = {0u, 0u};

@@ -3,7 +3,7 @@
 // serialise LbmConfig (src/lbm/mod.rs:45-101) with serde_json: an object with
 // the struct's field names (including the reference's spelling
 // "ext_equilibrium_boudaries"), unit enum variants as strings ("D3Q19",
-// "Srt", "FP16S", propellant "H"), the nested Units (src/lbm/units.rs:12-25)
+// "Srt", "FP16S", propellant "H"), the nested Units (src/lbm/units.rs:14-27)
 // and GraphicsConfig (src/lbm/graphics.rs:101-156).
 //
 // Reading takes every LbmConfig field it knows, maps

@@ -462,7 +462,7 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t brick, c
     for (; c < nchunks; c++) {
         const uint32_t buf = c & 1u;
         if (threadIdx.x == 0 && c + 1 < nchunks) eb_issue(L, sm, c + 1, last);
-        const bool landed = mbar_wait(&sm.bar[buf], uses[buf] & 1u, WAIT_LIMIT);
+        const bool landed = mbar_wait(&sm.bar[buf], uses[buf] & 1u, L.wait_limit);
         ok = __syncthreads_and(landed) != 0;  // block-uniform
         if (!ok) break;
         uses[buf]++;

@@ -64,7 +64,7 @@ void api_count_launches(uint64_t n) { g_launches += n; }
 namespace {
 
 // ---------------------------------------------------------------------------
-// Units -> kernel constants (src/lbm/units.rs:259-307; domain.rs:808, 839, 848),
+// Units -> kernel constants (src/lbm/units.rs:149-197; domain.rs:808, 839, 848),
 // evaluated in the same f32/f64 steps as the Rust code.
 // ---------------------------------------------------------------------------
 float sqf(float x) { return x * x; }
@@ -430,7 +430,7 @@ int ion_units_default(ion_units* u) {
 int ion_units_set(ion_units* u, float lbm_length, float lbm_velocity, float lbm_rho, float lbm_charge, float lbm_temp,
                   float si_length, float si_velocity, float si_rho, float si_charge, float si_temp) {
     if (!u) return fail(ION_E_INVALID, "null units");
-    u->m = si_length / lbm_length;                  // src/lbm/units.rs:164-168
+    u->m = si_length / lbm_length;                  // src/lbm/units.rs:54-58
     u->kg = si_rho / lbm_rho * cbf(u->m);
     u->s = u->m / (si_velocity / lbm_velocity);
     u->a = si_charge / lbm_charge / u->s;
@@ -603,6 +603,13 @@ int ion_lbm_set_electron_background(ion_lbm* h, float rho_e0) {
     if (!h->cfg.ext_magneto_hydro) return fail(ION_E_STATE, "the electron background applies to ext_magneto_hydro");
     if (!(rho_e0 >= 0.0f) || !std::isfinite(rho_e0)) return fail(ION_E_INVALID, "rho_e0 must be finite and >= 0");
     h->L.rho_e0 = rho_e0;
+    return ION_OK;
+}
+
+int ion_lbm_set_wait_limit(ion_lbm* h, uint32_t polls) {
+    if (!h) return fail(ION_E_INVALID, "null handle");
+    h->L.wait_limit = polls;
+    h->graph_dirty = true;  // the captured launches hold the old value
     return ION_OK;
 }
 
@@ -811,6 +818,19 @@ int ion_lbm_mesh_translate(ion_lbm* h, uint32_t index, float dx, float dy, float
         for (uint32_t i = 0; i < m.ntri; i++)
             for (int a = 0; a < 3; a++) (*p)[3 * (size_t)i + a] += d[a];
     for (int a = 0; a < 3; a++) { m.center[a] += d[a]; m.pmin[a] += d[a]; m.pmax[a] += d[a]; }
+    return ION_OK;
+}
+
+int ion_lbm_mesh_triangles(const ion_lbm* h, uint32_t index, float* p0, float* p1, float* p2, uint32_t capacity,
+                           uint32_t* ntri) {
+    if (!h || index >= h->meshes.size()) return fail(ION_E_INVALID, "no mesh %u", index);
+    const HostMesh& m = h->meshes[index];
+    if (ntri) *ntri = m.ntri;
+    if (!p0 && !p1 && !p2) return ION_OK;  // size query
+    if (!p0 || !p1 || !p2 || capacity < m.ntri) return fail(ION_E_INVALID, "mesh %u has %u triangles", index, m.ntri);
+    memcpy(p0, m.p0.data(), sizeof(float) * 3 * (size_t)m.ntri);
+    memcpy(p1, m.p1.data(), sizeof(float) * 3 * (size_t)m.ntri);
+    memcpy(p2, m.p2.data(), sizeof(float) * 3 * (size_t)m.ntri);
     return ION_OK;
 }
 
@@ -1191,6 +1211,12 @@ int ion_lbm_reset_kernel_time(ion_lbm* h) {
 // ---- batches of independent domains (batch_kernels.cu) -----------------------
 }  // extern "C"
 
+namespace {
+constexpr uint32_t BARRIER_LIMIT = 1u << 26;  // polls (64 ns apart) before a grid barrier gives up
+static_assert(BARRIER_LIMIT == ION_BARRIER_LIMIT_DEFAULT && WAIT_LIMIT == ION_WAIT_LIMIT_DEFAULT,
+              "the header's documented defaults");
+}
+
 struct ion_batch {
     std::vector<ion_lbm*> doms;
     int ft = ION_FP32;
@@ -1204,6 +1230,7 @@ struct ion_batch {
     uint32_t* d_bin_off = nullptr;
     uint32_t total_bins = 0;
     uint32_t* d_sync = nullptr;  // [0] barrier count, [1] barrier generation, [2] error
+    uint32_t barrier_limit = BARRIER_LIMIT;
     uint64_t t = 0;
     int sms = 0;
     bool tuned = false;
@@ -1234,6 +1261,7 @@ BatchDev batch_view(ion_batch* b, uint32_t block) {
     B.bar_count = b->d_sync;
     B.bar_gen = b->d_sync + 1;
     B.err = b->d_sync + 2;
+    B.barrier_limit = b->barrier_limit;
     return B;
 }
 
@@ -1416,6 +1444,22 @@ int ion_batch_run(ion_batch* b, uint64_t steps) {
         if (rc) return rc;
     }
     for (ion_lbm* h : b->doms) h->t += total;
+    return ION_OK;
+}
+
+int ion_batch_set_wait_limits(ion_batch* b, uint32_t barrier_polls, uint32_t tile_polls) {
+    if (!b) return fail(ION_E_INVALID, "null batch");
+    CK(cudaStreamSynchronize(b->stream));
+    b->barrier_limit = barrier_polls;
+    std::vector<DevLbm> views(b->doms.size());
+    for (size_t i = 0; i < b->doms.size(); i++) {
+        b->doms[i]->L.wait_limit = tile_polls;
+        b->doms[i]->graph_dirty = true;
+        views[i] = b->doms[i]->L;
+    }
+    CK(cudaMemcpy(b->d_doms, views.data(), sizeof(DevLbm) * views.size(), cudaMemcpyHostToDevice));
+    if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }  // holds the old barrier limit
+    b->graph_failed = false;
     return ION_OK;
 }
 

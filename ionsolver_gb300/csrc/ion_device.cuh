@@ -161,7 +161,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
     return false;
 }
 
-constexpr uint32_t WAIT_LIMIT = 1u << 24;  // polls before a wait gives up
+// Polls before a wait for staged data gives up (the default of DevLbm::wait_limit).
+// A wait that gives up records an error and skips its tile; the copies still in
+// flight are then waited for with this full limit before the block exits.
+constexpr uint32_t WAIT_LIMIT = 1u << 24;
 
 template <int FT> struct Ddf;
 template <> struct Ddf<ION_FP32> {

@@ -51,6 +51,7 @@ struct BatchDev {
     uint32_t* bar_count;
     uint32_t* bar_gen;
     uint32_t* err;
+    uint32_t barrier_limit;  // polls before a grid barrier gives up
 };
 int batch_max_blocks_per_sm(int ft, bool mhd, bool fast, int block);
 cudaError_t launch_batch_step(const BatchDev& B, int ft, bool mhd, bool fast, uint32_t grid, uint32_t block,

@@ -550,7 +550,7 @@ __global__ void __launch_bounds__(256, 2) k_sc_rows(const DevLbm L, const uint32
         const uint32_t b = k & 1u;
         // the other buffer was released at the end of the previous row
         if (threadIdx.x == 0 && r + gridDim.x < nrows) stage(r + gridDim.x, b ^ 1u);
-        ok = mbar_wait(&bar[b], (k >> 1) & 1u, WAIT_LIMIT);
+        ok = mbar_wait(&bar[b], (k >> 1) & 1u, L.wait_limit);
         if (!__syncthreads_and(ok)) break;
         const uint8_t* buf = rows_smem + b * RB;
         const uint32_t y = r % ny, z = r / ny;
@@ -569,10 +569,11 @@ __global__ void __launch_bounds__(256, 2) k_sc_rows(const DevLbm L, const uint32
     }
 }
 
-// waits for an mbarrier phase; gives up after WAIT_LIMIT polls (setting *fail) or as
-// soon as another warp has set *fail
-__device__ __forceinline__ bool mbar_wait_or_fail(uint64_t* bar, uint32_t parity, volatile uint32_t* fail) {
-    for (uint32_t i = 0; i < WAIT_LIMIT; i++) {
+// waits for an mbarrier phase; gives up after `limit` polls (setting *fail) or as soon
+// as another warp has set *fail
+__device__ __forceinline__ bool mbar_wait_or_fail(uint64_t* bar, uint32_t parity, volatile uint32_t* fail,
+                                                  uint32_t limit) {
+    for (uint32_t i = 0; i < limit; i++) {
         uint32_t done;
         asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
                      : "=r"(done) : "r"(smem_addr(bar)), "r"(parity) : "memory");
@@ -614,7 +615,7 @@ __global__ void __launch_bounds__(288, MHD ? 2 : 3) k_sc_rows_ws(const DevLbm L,
         if (threadIdx.x == nct) {
             for (uint32_t k = 0; k < my_rows; k++) {
                 const uint32_t b = k & 1u, r = blockIdx.x + k * gridDim.x;
-                if (k >= 2 && !mbar_wait_or_fail(&empty[b], ((k - 2) >> 1) & 1u, fail)) break;
+                if (k >= 2 && !mbar_wait_or_fail(&empty[b], ((k - 2) >> 1) & 1u, fail, L.wait_limit)) break;
                 if (*fail) break;
                 uint8_t* dst = rows_smem + b * RB;
                 const uint32_t y = r % ny, z = r / ny, own = (y + z * ny) * nx;
@@ -648,7 +649,7 @@ __global__ void __launch_bounds__(288, MHD ? 2 : 3) k_sc_rows_ws(const DevLbm L,
         const uint32_t lane = threadIdx.x & 31u;
         for (uint32_t k = 0; k < my_rows; k++) {
             const uint32_t b = k & 1u, r = blockIdx.x + k * gridDim.x;
-            const bool go = mbar_wait_or_fail(&full[b], (k >> 1) & 1u, fail) && *fail == 0u;
+            const bool go = mbar_wait_or_fail(&full[b], (k >> 1) & 1u, fail, L.wait_limit) && *fail == 0u;
             if (go) {
                 const uint8_t* buf = rows_smem + b * RB;
                 const uint32_t y = r % ny, z = r / ny;

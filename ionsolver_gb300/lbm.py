@@ -71,7 +71,7 @@ class ModelType:
 
 @dataclass
 class Units:
-    """Units (src/lbm/units.rs:122-307): lattice unit * factor = SI unit."""
+    """Units (src/lbm/units.rs:14-197): lattice unit * factor = SI unit."""
     m: float = 1.0
     kg: float = 1.0
     s: float = 1.0
@@ -220,6 +220,10 @@ class Lbm:
         electron gas at density rho_e0, charge lattice at Q + rho_e0."""
         N.check(N.lib().ion_lbm_set_electron_background(self._h, float(rho_e0)))
 
+    def set_wait_limit(self, polls: int | None = None) -> None:
+        """Polls before a device wait for staged data gives up (None: the default)."""
+        N.check(N.lib().ion_lbm_set_wait_limit(self._h, N.ION_WAIT_LIMIT_DEFAULT if polls is None else int(polls)))
+
     def do_time_step(self) -> None:
         N.check(N.lib().ion_lbm_do_time_step(self._h))
 
@@ -288,6 +292,15 @@ class Lbm:
 
     def mesh_translate(self, index: int, d: Sequence[float]) -> None:
         N.check(N.lib().ion_lbm_mesh_translate(self._h, index, float(d[0]), float(d[1]), float(d[2])))
+
+    def mesh_triangles(self, index: int) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """The mesh's vertex arrays p0, p1, p2, each [ntri][3] float32."""
+        nt = C.c_uint32()
+        N.check(N.lib().ion_lbm_mesh_triangles(self._h, index, None, None, None, 0, C.byref(nt)))
+        p = [np.empty((nt.value, 3), np.float32) for _ in range(3)]
+        N.check(N.lib().ion_lbm_mesh_triangles(self._h, index, p[0].ctypes.data, p[1].ctypes.data, p[2].ctypes.data,
+                                               nt.value, C.byref(nt)))
+        return p[0], p[1], p[2]
 
     def mesh_bounds(self, index: int) -> dict:
         out = (C.c_float * 9)()
@@ -471,6 +484,12 @@ class Batch:
 
     def run(self, steps: int) -> None:
         N.check(N.lib().ion_batch_run(self._h, int(steps)))
+
+    def set_wait_limits(self, barrier_polls: int | None = None, tile_polls: int | None = None) -> None:
+        """Poll limits of the batch step's grid barriers and staged-tile waits (None: the defaults)."""
+        N.check(N.lib().ion_batch_set_wait_limits(
+            self._h, N.ION_BARRIER_LIMIT_DEFAULT if barrier_polls is None else int(barrier_polls),
+            N.ION_WAIT_LIMIT_DEFAULT if tile_polls is None else int(tile_polls)))
 
     def finish(self, timeout_ms: int = -1) -> None:
         N.check(N.lib().ion_batch_finish(self._h, int(timeout_ms)))

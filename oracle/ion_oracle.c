@@ -188,7 +188,7 @@ static void st(const orc* h, void* p, uint64_t i, R x) {
 }
 
 /* ------------------------------------------------------------------------
- * Units -> kernel constants: src/lbm/units.rs:259-307 (f32 arithmetic as in
+ * Units -> kernel constants: src/lbm/units.rs:149-197 (f32 arithmetic as in
  * Rust, f64 parts where the reference computes in f64), DEF_W
  * (src/lbm/domain.rs:808), DEF_KMU (839), DEF_WQ (848).
  * ---------------------------------------------------------------------- */
@@ -219,7 +219,7 @@ int orc_constants(const ion_config* c, ion_constants* k) {
     k->kimg = (float)((1.0 / (atom_mass(u->prop) * 1e20)) / (double)u->kg);
     k->kvev = (float)(9.1093837139E-31 / (2.0 * 1.602176634E-19) / (double)u->kg);
     k->kme = (float)(5.68563006E-12 / ((double)u->kg / ((double)u->a * (double)u->s)));
-    k->wq = 1.0f / (2.0f * 1.0f + 0.5f); /* k_charge_expansion_lu() = 1 (units.rs:279-283) */
+    k->wq = 1.0f / (2.0f * 1.0f + 0.5f); /* k_charge_expansion_lu() = 1 (units.rs:169-173) */
     /* SUBGRID_ECR: kkBme_lu, keabs_lu (units.rs:187-193), f64 arithmetic rounded to f32 */
     k->kkbme = (float)(-22734499.72063751808909449412 /
                        (((double)u->m * (double)u->m) / (((double)u->s * (double)u->s) * (double)u->k)));

@@ -94,7 +94,7 @@ void set_globals(const RefLbm* h) {
     g_kkbme = h->k.kkbme; g_keabs = h->k.keabs;
 }
 
-// Units::magnetization_si_lu / charge_si_lu, src/lbm/units.rs:240-257
+// Units::magnetization_si_lu / charge_si_lu, src/lbm/units.rs:130-133, 145-147
 float magnetization_si_lu(const ion_units& u, float m) { return m / (u.a / u.m); }
 float charge_si_lu(const ion_units& u, float q) { return q / (u.a * u.s); }
 

@@ -1,4 +1,4 @@
-"""Kernel constants from Units (IonSolver src/lbm/units.rs:259-307,
+"""Kernel constants from Units (IonSolver src/lbm/units.rs:149-197,
 src/lbm/domain.rs:808-848): the library, the oracle and an independent
 numpy float32 restatement agree bit for bit."""
 import numpy as np
