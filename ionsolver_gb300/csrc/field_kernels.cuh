@@ -241,10 +241,14 @@ struct FastSrc {
     float4 d[7];
 };
 
-__device__ __forceinline__ void fast_src(FastSrc& f, float4 p, float4 v, float ox, float oy, float oz) {
+// A source of the brick's near box (summed directly, see eb_tile) enters the far sums
+// as q = 0 at p' = 0 with |p'|^2 = 1: |R|^2 = |c'|^2 + 1 >= 1 stays finite, so it
+// adds exactly zero (the cell's own bin, possibly at |R| = 0, is one of them).
+__device__ __forceinline__ void fast_src(FastSrc& f, float4 p, float4 v, float ox, float oy, float oz, bool in_box) {
     // p = bin centre, v = (q, vx, vy, vz)
+    if (in_box) { p = make_float4(ox, oy, oz, 0.0f); v = make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
     const float px = p.x - ox, py = p.y - oy, pz = p.z - oz;
-    const float pp = fmaf(pz, pz, fmaf(py, py, px * px));
+    const float pp = in_box ? 1.0f : fmaf(pz, pz, fmaf(py, py, px * px));
     const float q = v.x;
     const float qx = q * v.y, qy = q * v.z, qz = q * v.w;
     const float wx = qy * pz - qz * py, wy = qz * px - qx * pz, wz = qx * py - qy * px;
@@ -330,6 +334,32 @@ __device__ __forceinline__ void far_finish(const Pair3& c, const FarSums& f, boo
     b[1] = b[1] + ((Az * cx - Ax * cz) - Wy);
     b[2] = b[2] + ((Ax * cy - Ay * cx) - Wz);
 }
+
+// One source of the near box for a cell pair, directly: R = c - p per lane (exact),
+// q R/|R|^3 and (q v x R)/|R|^3 added to the pair's sums.  A lane that must skip the
+// source (its own bin, or an inactive cell) gets |R|^2 = 1 and weight 0, so it adds
+// exact zeros.
+__device__ __forceinline__ void near_pair(P2 rx, P2 ry, P2 rz, float4 v, bool use_lo, bool use_hi, Pair3& e,
+                                          Pair3& b) {
+    const P2 r2 = fma2(rz, rz, fma2(ry, ry, mul2(rx, rx)));
+    float i0, i1;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(i0) : "f"(use_lo ? lo32(r2) : 1.0f));
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(i1) : "f"(use_hi ? hi32(r2) : 1.0f));
+    const P2 inv = pk(i0, i1);
+    const P2 w = mul2(mul2(mul2(inv, inv), inv), pk(use_lo ? 1.0f : 0.0f, use_hi ? 1.0f : 0.0f));
+    const P2 s = mul2(pk(v.x, v.x), w);
+    e.x = fma2(s, rx, e.x);
+    e.y = fma2(s, ry, e.y);
+    e.z = fma2(s, rz, e.z);
+    const P2 qx = pk(v.y, v.y), qy = pk(v.z, v.z), qz = pk(v.w, v.w);
+    const P2 cx = fma2(qy, rz, mul2(pk(-v.w, -v.w), ry));
+    const P2 cy = fma2(qz, rx, mul2(pk(-v.y, -v.y), rz));
+    const P2 cz = fma2(qx, ry, mul2(pk(-v.z, -v.z), rx));
+    b.x = fma2(w, cx, b.x);
+    b.y = fma2(w, cy, b.y);
+    b.z = fma2(w, cz, b.z);
+}
+constexpr uint32_t NEAR_BATCH = 256;  // near-box bins staged at a time (2 float4 each, within sm.fast)
 
 // Shared-memory staging area of one thread block; the mbarrier phase of each
 // buffer is tracked in `uses` so one block can process many tiles.
@@ -443,6 +473,68 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t brick, c
         for (int c = 0; c < 3; c++) { e[k][c] = 0.0f; b[k][c] = 0.0f; }
         if (active[k]) near_field<FAST>(L, n, x, y, z, e[k], b[k]);
     }
+    // FAST: the bins within one bin (Chebyshev) of the brick's cells -- its near box --
+    // are summed directly, q R/|R|^3 with R = c - p exact (cell and bin coordinates are
+    // integers and halves), each cell skipping its own bin.  For such a close source the
+    // far sums' split E = c' S - P (below) cancels, which costs up to 10x the rounding
+    // error of the direct form; the far loop sees these bins with q = 0 (fast_src).
+    uint32_t box_lo[3] = {0u, 0u, 0u}, box_hi[3] = {0u, 0u, 0u};
+    if constexpr (FAST) {
+        // the whole brick's box, also for a half-brick block: every cell then sums the
+        // same sources directly, whatever the block shape (batches pick 128 or 256)
+        const uint32_t lo[3] = {bx * EB_BX, by * EB_BY, bz * EB_CPT};
+        const uint32_t hi[3] = {min(lo[0] + EB_BX, L.nx) - 1u, min(lo[1] + EB_BY, L.ny) - 1u, min(lo[2] + EB_CPT, L.nz) - 1u};
+        const uint32_t bsz[3] = {L.bsx ? L.bsx : 1u, L.bsy ? L.bsy : 1u, L.bsz ? L.bsz : 1u};
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const uint32_t b0 = lo[a] / bsz[a], b1 = hi[a] / bsz[a];
+            box_lo[a] = b0 > 0u ? b0 - 1u : 0u;
+            box_hi[a] = min(b1 + 1u, L.nd - 1u);
+        }
+        // The box's bins are staged in shared memory (sm.fast is free until the far loop)
+        // in batches of NEAR_BATCH; every thread then sums them for its cells, the pair
+        // (2j, 2j+1) -- the same x and y, z one apart -- in packed instructions.
+        const uint32_t first = L.first_src, last = src_last<FAST>(L);
+        const uint32_t ex = box_hi[0] - box_lo[0] + 1u, ey = box_hi[1] - box_lo[1] + 1u;
+        const uint32_t nbox = ex * ey * (box_hi[2] - box_lo[2] + 1u);
+        float4* stage = reinterpret_cast<float4*>(sm.fast);  // [NEAR_BATCH] centres + index, then (q, q v)
+        Pair3 en[NP], bn[NP];
+#pragma unroll
+        for (uint32_t j = 0; j < NP; j++) { en[j] = {0ull, 0ull, 0ull}; bn[j] = en[j]; }
+        const P2 px2 = pk(ax[0], ax[0]), py2 = pk(ay[0], ay[0]);
+        for (uint32_t b0 = 0; b0 < nbox; b0 += NEAR_BATCH) {
+            const uint32_t cnt = min(NEAR_BATCH, nbox - b0);
+            __syncthreads();  // the previous batch is consumed
+            for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) {
+                const uint32_t t = b0 + i;
+                const uint32_t d = (box_lo[0] + t % ex) + ((box_lo[1] + (t / ex) % ey) + (box_lo[2] + t / (ex * ey)) * L.nd) * L.nd;
+                const float4 pd = L.lod_pos[d], v = reinterpret_cast<const float4*>(L.qu_lod)[d];
+                const bool src = d >= first && d < last;  // inside the reference's source range
+                stage[i] = make_float4(pd.x, pd.y, pd.z, __uint_as_float(d));
+                stage[NEAR_BATCH + i] = src ? make_float4(v.x, v.x * v.y, v.x * v.z, v.x * v.w) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
+            __syncthreads();
+            for (uint32_t i = 0; i < cnt; i++) {
+                const float4 pd = stage[i], v = stage[NEAR_BATCH + i];
+                const uint32_t d = __float_as_uint(pd.w);
+                const P2 rx = add2(px2, pk(-pd.x, -pd.x)), ry = add2(py2, pk(-pd.y, -pd.y));
+#pragma unroll
+                for (uint32_t j = 0; j < NP; j++)
+                    near_pair(rx, ry, pk(az[2 * j] - pd.z, az[2 * j + 1] - pd.z), v,
+                              active[2 * j] && d != own[2 * j], active[2 * j + 1] && d != own[2 * j + 1], en[j], bn[j]);
+            }
+        }
+        __syncthreads();  // sm.fast is written by the far loop next
+#pragma unroll
+        for (uint32_t j = 0; j < NP; j++)
+#pragma unroll
+            for (uint32_t h = 0; h < 2; h++) {
+                float* ek = e[2 * j + h];
+                float* bk = b[2 * j + h];
+                ek[0] = ek[0] + half(en[j].x, h); ek[1] = ek[1] + half(en[j].y, h); ek[2] = ek[2] + half(en[j].z, h);
+                bk[0] = bk[0] + half(bn[j].x, h); bk[1] = bk[1] + half(bn[j].y, h); bk[2] = bk[2] + half(bn[j].z, h);
+            }
+    }
     Pair3 cp[NP];  // FAST: the relative coordinates in pairs, and |c'|^2
     P2 cc[NP];
 #pragma unroll
@@ -474,7 +566,12 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t brick, c
         const bool any_own = __any_sync(0xFFFFFFFFu, here);  // this chunk holds some cell's own bin
         if constexpr (FAST) {
             for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x)
-                fast_src(sm.fast[k], sm.pos[buf][k], sm.val[buf][k], ox, oy, oz);
+            {
+                const uint32_t d = base + k, dx = d % L.nd, dy = (d / L.nd) % L.nd, dz = d / (L.nd * L.nd);
+                const bool in_box = dx >= box_lo[0] && dx <= box_hi[0] && dy >= box_lo[1] && dy <= box_hi[1] &&
+                                    dz >= box_lo[2] && dz <= box_hi[2];
+                fast_src(sm.fast[k], sm.pos[buf][k], sm.val[buf][k], ox, oy, oz, in_box);
+            }
             __syncthreads();
             const FastSrc* src = sm.fast;
             if (any_own) {

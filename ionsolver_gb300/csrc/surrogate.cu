@@ -603,7 +603,7 @@ __global__ void __launch_bounds__(SC_THREADS, 2) k_surrogate_cells(const DevLbm 
             const uint32_t m = __ballot_sync(0xFFFFFFFFu, ok);
             if (ok) {  // coordinates relative to this bin's centre
                 const float4 o = L.lod_pos[bin];
-                fast_src(sm.src[cnt + __popc(m & ((1u << lane) - 1u))], L.lod_pos[d], qu[d], o.x, o.y, o.z);
+                fast_src(sm.src[cnt + __popc(m & ((1u << lane) - 1u))], L.lod_pos[d], qu[d], o.x, o.y, o.z, false);
             }
             cnt += __popc(m);
         }

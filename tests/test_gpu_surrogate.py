@@ -10,6 +10,7 @@ reproducing the exact FAST field bit for bit."""
 import numpy as np
 import pytest
 
+import ionsolver_gb300 as I
 from ionsolver_gb300 import workloads as W
 from oracle import surrogate_ref as S
 from tests import _util as U
@@ -193,3 +194,52 @@ def test_tcgen05_convolution_matches_mma_sync(nd, cin, cout, dil):
     N.check(N.lib().ion_check_tcgen05_conv(nd, cin, cout, dil, 0x5eed + nd + cin + cout + dil, C.byref(err)))
     print(f"\ntcgen05 conv nd {nd} cin {cin} cout {cout} dil {dil}: max rel {err.value:.3e}")
     assert 0.0 <= err.value < 1e-3
+
+
+def _plasma_case(field_mode=2, float_type=0):
+    return W.mhd_plasma(n=64, depth=3, magnet_r=10.0, magnet_t=6.0, field_mode=field_mode, float_type=float_type)
+
+
+def test_learned_field_run_against_the_float64_oracle(tmp_path):
+    """The configuration-4 path end to end on the finite-plasma start at 64^3
+    (depth 3, FP16S storage, learned far field with the sampled check and
+    fallback, a network trained on this grid), 50 steps:
+    * the gas velocity is within 1e-3 (max |diff| / max |u|) of the float64
+      oracle's exact-field run of the same inputs;
+    * the field the network gives at step 50 is within 1e-2 of the exact FAST
+      field of the same state (the 49-step state restored from a checkpoint and
+      stepped once with the exact field), for E and B.
+    Against the float64 oracle the E field of any FP16S run, exact field
+    included, is dominated by the storage (test_gpu_accuracy.py): 16-bit DDFs
+    do not resolve the net charge of this state."""
+    steps = 50
+    case = _plasma_case()
+    g = U.setup_gpu(case)
+    g.surrogate_train(samples=480, epochs=16, batch=8, lr=2e-3, seed=5)
+    g.surrogate_configure(tolerance=1e-2, check_cells=1024)
+    g.initialize()
+    g.run(steps - 1)
+    p = tmp_path / "s49.ion"
+    g.checkpoint(p)
+    g.do_time_step()
+    g.finish_queues(120000)
+    st = g.surrogate_stats()
+    x = I.Lbm.restore(p)
+    x.set_field_mode(1)  # the exact FAST sum on the same state
+    x.do_time_step()
+    x.finish_queues(120000)
+    for name in ("fi", "fqi", "ei", "qu_lod"):  # the same sources
+        assert U.bit_diff(g.read(name), x.read(name)) == 0, name
+    ref_case = _plasma_case(field_mode=0, float_type=2)
+    o = U.setup_oracle(ref_case, kind="f64")
+    U.initialize_oracle(o, ref_case)
+    o.run(steps)
+    n = 64 ** 3
+    u_err = U.rel_err(g.read("u"), o.field("u"))
+    e_err = U.rel_err(g.read("e_dyn")[:3 * n], x.read("e_dyn")[:3 * n])
+    b_err = U.rel_err(g.read("b_dyn"), x.read("b_dyn"))
+    print(f"\nlearned field, plasma 64^3 FP16S, {steps} steps: u vs FP64 {u_err:.3e}; step-{steps} field vs exact "
+          f"on the same state: E {e_err:.3e}, B {b_err:.3e}; checks {st['checks']} fallbacks {st['fallbacks']}")
+    assert np.isfinite(g.read("u")).all() and st["nonfinite"] == 0
+    assert u_err <= 1e-3, u_err
+    assert e_err <= 1e-2 and b_err <= 1e-2, (e_err, b_err)
