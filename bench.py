@@ -69,7 +69,7 @@ FLOP_PER_INTERACTION = 34  # one source's E and B: 34 FLOP + 1 sqrt (sim_kernels
 # (rings384: the rings288 capture of k_sc_rows scaled by the cell count, (384/288)^3; every
 # stream is read and written once per cell, so the traffic is proportional to the cells)
 NCU_TRAFFIC = {("tgv256", "k_sc_rows_ws"): 2.506631e9, ("mhd128", "k_sc_rows_ws"): 0.807230e9,
-               ("mhd128", "k_update_e_b_fast"): 64.001e6, ("rings384", "k_sc_rows"): 64 / 27 * 5.628695e9}
+               ("mhd128", "k_update_e_b_fast"): 63.815e6, ("rings384", "k_sc_rows"): 64 / 27 * 5.628695e9}
 
 
 def stencil_kernel(cfg: dict) -> str:

@@ -182,49 +182,6 @@ __device__ __forceinline__ void add_src(float rx, float ry, float rz, float4 val
     }
 }
 
-// Packed FP32 pairs (PTX add/mul/fma .f32x2, sm_100 and later): one
-// instruction does the same IEEE round-to-nearest operation on the two
-// halves of a 64-bit register, so two cells advance through one source with
-// half the issue slots and bit for bit the values of the scalar code.  A pair
-// lives in a 64-bit integer (low half = first cell) from load to store, so no
-// packing moves are needed between the instructions.
-using P2 = unsigned long long;
-__device__ __forceinline__ P2 pk(float lo, float hi) {
-    P2 r;
-    asm("mov.b64 %0, {%1,%2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-// (the unpack writes both halves; the unused one draws warning 550)
-#pragma nv_diag_suppress 550
-__device__ __forceinline__ float lo32(P2 v) {
-    float a, b;
-    asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-    return a;
-}
-__device__ __forceinline__ float hi32(P2 v) {
-    float a, b;
-    asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-    return b;
-}
-#pragma nv_diag_default 550
-__device__ __forceinline__ float half(P2 v, bool hi) { return hi ? hi32(v) : lo32(v); }
-__device__ __forceinline__ void set_half(P2& v, bool hi, float x) { v = hi ? pk(lo32(v), x) : pk(x, hi32(v)); }
-__device__ __forceinline__ P2 add2(P2 a, P2 b) {
-    P2 d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ P2 mul2(P2 a, P2 b) {
-    P2 d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ P2 fma2(P2 a, P2 b, P2 c) {
-    P2 d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-
 // FAST far field in coordinates relative to an origin o near the cells (the
 // centre of their brick): with c' = c - o and p' = p - o,
 //   |R|^2 = (|c'|^2 + |p'|^2) - 2 c'.p'                 (4 operations, no R,

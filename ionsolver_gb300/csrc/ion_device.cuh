@@ -134,6 +134,60 @@ __host__ __device__ __forceinline__ float fp16c_decode(uint16_t x) {
     return bitsf(sign | (mag >= 0x0800u ? nrm : sub));
 }
 
+// Packed FP32 pairs (PTX add/sub/mul/fma .f32x2, sm_100 and later): one
+// instruction does the same IEEE round-to-nearest operation on the two halves
+// of a 64-bit register (each instruction checked against the scalar one on the
+// device), so two cells advance with half the issue slots.  A pair lives in a
+// 64-bit integer (low half = first cell) from load to store, so no packing moves
+// are needed between the instructions.  One caveat, measured on GB300 with CUDA
+// 13.0: ptxas contracts a packed multiply that feeds a packed add into a packed
+// FMA even under --fmad=false (which it honours for scalar code), also when the
+// multiply is written as an FMA with a -0 addend or as volatile asm.  So packed
+// code is only bit-identical to the scalar form where no inexact product feeds an
+// addition; the FAST field, which uses these, is an approximation anyway.
+using P2 = unsigned long long;
+__device__ __forceinline__ P2 pk(float lo, float hi) {
+    P2 r;
+    asm("mov.b64 %0, {%1,%2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+// (the unpack writes both halves; the unused one draws warning 550)
+#pragma nv_diag_suppress 550
+__device__ __forceinline__ float lo32(P2 v) {
+    float a, b;
+    asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+    return a;
+}
+__device__ __forceinline__ float hi32(P2 v) {
+    float a, b;
+    asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+    return b;
+}
+#pragma nv_diag_default 550
+__device__ __forceinline__ float half(P2 v, bool hi) { return hi ? hi32(v) : lo32(v); }
+__device__ __forceinline__ void set_half(P2& v, bool hi, float x) { v = hi ? pk(lo32(v), x) : pk(x, hi32(v)); }
+__device__ __forceinline__ P2 add2(P2 a, P2 b) {
+    P2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ P2 mul2(P2 a, P2 b) {
+    P2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ P2 fma2(P2 a, P2 b, P2 c) {
+    P2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+__device__ __forceinline__ P2 sub2(P2 a, P2 b) {
+    P2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
 // shared memory, mbarriers and bulk asynchronous copies (cp.async.bulk, completion
 // counted in bytes on an mbarrier)
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
