@@ -566,7 +566,7 @@ def main():
         lbm.finish_queues(600000)
         lbm.reset_kernel_time()
     else:
-        batch.run(max(a.warmup, 1) + 2 * 4)  # includes the autotuner's trial steps
+        batch.run(max(a.warmup, 1) + 2 * 8)  # includes the autotuner's trial steps (2 per launch shape)
         batch.finish(600000)
     launches0 = I.kernel_launch_count()
     dist.barrier()

@@ -1252,8 +1252,8 @@ BatchDev batch_view(ion_batch* b, uint32_t block) {
     BatchDev B{};
     B.doms = b->d_doms;
     B.ndom = (uint32_t)b->doms.size();
-    B.tile_off = b->d_tile_off[block_slot(block)];
-    B.total_tiles = b->total_tiles[block_slot(block)];
+    B.tile_off = b->d_tile_off[block_slot(BATCH_SC_THREADS)];  // the stencil kernel's block size
+    B.total_tiles = b->total_tiles[block_slot(BATCH_SC_THREADS)];
     B.brick_off = b->d_brick_off[block_slot(block)];
     B.total_bricks = b->total_bricks[block_slot(block)];
     B.bin_off = b->d_bin_off;
@@ -1268,7 +1268,7 @@ BatchDev batch_view(ion_batch* b, uint32_t block) {
 int batch_launch(ion_batch* b, uint32_t block, uint32_t grid) {
     const cudaError_t e = launch_batch_step(batch_view(b, block), b->ft, b->mhd, b->fast, grid, block, b->t, b->stream);
     if (e != cudaSuccess) return fail(ION_E_CUDA, "batch step launch: %s", cudaGetErrorString(e));
-    g_launches++;
+    g_launches += b->mhd ? 2 : 1;
     b->t += 1;
     return ION_OK;
 }
@@ -1435,7 +1435,7 @@ int ion_batch_run(ion_batch* b, uint64_t steps) {
     if (b->graph) {
         for (; steps >= 2; steps -= 2) {
             CK(cudaGraphLaunch(b->graph, b->stream));
-            g_launches += 2;
+            g_launches += b->mhd ? 4 : 2;
             b->t += 2;
         }
     }

@@ -53,6 +53,8 @@ struct BatchDev {
     uint32_t* err;
     uint32_t barrier_limit;  // polls before a grid barrier gives up
 };
+// threads per block of the batch's stencil kernel (its tiles: BATCH_SC_THREADS * EB_CPT cells)
+constexpr uint32_t BATCH_SC_THREADS = 128;
 int batch_max_blocks_per_sm(int ft, bool mhd, bool fast, int block);
 cudaError_t launch_batch_step(const BatchDev& B, int ft, bool mhd, bool fast, uint32_t grid, uint32_t block,
                               uint64_t t, cudaStream_t s);
