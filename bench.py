@@ -78,7 +78,7 @@ def stencil_kernel(cfg: dict) -> str:
     rows = cfg.get("velocity_set", 2) == 2 and not cfg.get("ext_subgrid_ecr") and cfg["n_x"] % 16 == 0
     if not rows:
         return "k_stream_collide"
-    return "k_sc_rows_ws" if cfg["n_x"] <= 256 else "k_sc_rows"
+    return "k_sc_rows_ws" if cfg["n_x"] <= 384 else "k_sc_rows"
 
 
 def parse():

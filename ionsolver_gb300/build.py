@@ -26,6 +26,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true",
               "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-v", f"-I{REPO / 'include'}", f"-I{CSRC}"]
 SOURCES = ["lbm_q19.cu", "lbm_q15.cu", "lbm_q9.cu", "field_kernels.cu", "setup_kernels.cu", "batch_kernels.cu",
            "noalloc.cu", "surrogate.cu", "config_json.cpp", "ion_api.cu"]
+# (source, object name, extra flags): one translation unit compiled more than once
+VARIANTS = [("lbm_q19_sc.cu", f"lbm_q19_sc_{ft.lower()}", [f"-DION_SC_FT=ION_{ft}"]) for ft in ("FP32", "FP16S", "FP16C")]
 
 
 def nvcc() -> str:
@@ -35,8 +37,8 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
-def _compile(src: Path, obj: Path) -> str:
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+def _compile(src: Path, obj: Path, extra: list[str] | None = None) -> str:
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *(extra or []), "-c", str(src), "-o", str(obj)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src.name}:\n{r.stdout}\n{r.stderr}")
@@ -50,19 +52,22 @@ def _stale(obj: Path, deps: list[Path]) -> bool:
 def build(force: bool = False, verbose: bool = False) -> Path:
     OUT.mkdir(parents=True, exist_ok=True)
     headers = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + [REPO / "include" / "ionsolver.h"]
+    units = [(s, Path(s).stem, []) for s in SOURCES] + VARIANTS
     jobs = []
-    for s in SOURCES:
+    for s, stem, extra in units:
         src = CSRC / s
-        obj = OUT / (src.stem + ".o")
+        obj = OUT / (stem + ".o")
         if force or _stale(obj, [src, *headers]):
-            jobs.append((src, obj))
+            jobs.append((src, obj, extra))
     if jobs:
+        # the largest units first, so the longest compile starts at once
+        jobs.sort(key=lambda j: 0 if j[0].name.startswith("lbm_q19") or j[0].name == "batch_kernels.cu" else 1)
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             logs = list(ex.map(lambda j: _compile(*j), jobs))
         (OUT / "ptxas.log").write_text("\n".join(logs))
         if verbose:
             print("\n".join(logs))
-    objs = [OUT / (Path(s).stem + ".o") for s in SOURCES]
+    objs = [OUT / (stem + ".o") for _, stem, _ in units]
     if force or jobs or not LIB.exists():
         tmp = LIB.with_suffix(f".{os.getpid()}.tmp")
         cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]

@@ -107,6 +107,17 @@ __host__ __device__ __forceinline__ float bitsf(uint32_t u) {
 #endif
 }
 
+// v >> s with shifts of 32 or more giving 0 (PTX shr clamps the shift amount)
+__host__ __device__ __forceinline__ uint32_t shr_clamped(uint32_t v, uint32_t s) {
+#ifdef __CUDA_ARCH__
+    uint32_t r;
+    asm("shr.b32 %0, %1, %2;" : "=r"(r) : "r"(v), "r"(s));
+    return r;
+#else
+    return s >= 32u ? 0u : v >> s;
+#endif
+}
+
 // A NaN is encoded as the canonical quiet NaN 0x7FFFFFFF would be (the bit
 // pattern NVIDIA hardware gives every NaN result), so the stored value does
 // not depend on where a NaN came from.  The reference's MHD step produces
@@ -115,22 +126,26 @@ __host__ __device__ __forceinline__ float bitsf(uint32_t u) {
 __host__ __device__ __forceinline__ uint16_t fp16c_encode(float x) {
     const uint32_t xb = fbits(x);
     const uint32_t b = (((xb & 0x7FFFFFFFu) > 0x7F800000u) ? 0x7FFFFFFFu : xb) + 0x800u;
-    const uint32_t e = (b & 0x7F800000u) >> 23, m = b & 0x007FFFFFu;
+    const uint32_t e = (b >> 23) & 0xFFu;
     // both candidates, then a select (no divergent branch when a warp mixes normal and
-    // subnormal results): normal for e > 112, subnormal (shift clamped into 12..23) for
-    // 100 < e <= 112, zero below
-    const uint32_t nrm = (((e - 112u) << 11) & 0x7800u) | (m >> 12);
-    const uint32_t es = e < 101u ? 101u : (e > 112u ? 112u : e);
-    const uint32_t sub = (((0x007FF800u + m) >> (124u - es)) + 1u) >> 1;
-    return (uint16_t)(((b & 0x80000000u) >> 16) | (e > 112u ? nrm : (e > 100u ? sub : 0u)));
+    // subnormal results).  Normal (e > 112): the exponent rebiased by -112 into 4 bits
+    // next to the top 11 mantissa bits, i.e. (b >> 12) - (112 << 11) in 15 bits.
+    // Subnormal: the 24-bit significand shifted by 124 - e, then halved with rounding;
+    // for e <= 100 the shift is 24 or more and the result 0, as the reference's
+    // (e > 100) factor gives.  Equal to the reference's expression for all 2^32 inputs.
+    const uint32_t nrm = ((b >> 12) - (112u << 11)) & 0x7FFFu;
+    const uint32_t sub = (shr_clamped((b & 0x007FFFFFu) + 0x007FF800u, 124u - e) + 1u) >> 1;
+    return (uint16_t)(((b >> 16) & 0x8000u) | (e > 112u ? nrm : sub));
 }
 __host__ __device__ __forceinline__ float fp16c_decode(uint16_t x) {
     const uint32_t mag = x & 0x7FFFu, sign = (uint32_t)(x & 0x8000u) << 16;
-    // exponent field > 0: sign | (e + 112) << 23 | m << 12, one shift and one add;
-    // exponent field 0: m * 2^-25 exactly (m < 2^11), which is the normalised float the
-    // leading-zero count would build
+    // exponent field > 0: sign | (e + 112) << 23 | m << 12, one shift and one add.
+    // Exponent field 0: the same bits read as a float are 2^-15 + m 2^-26, so
+    // 2 (that) - 2^-14 = m 2^-25 exactly (one FMA, no integer conversion), which is the
+    // normalised float the reference's leading-zero count builds.  Equal to the
+    // reference's decoder for all 2^16 inputs.
     const uint32_t nrm = (mag << 12) + (112u << 23);
-    const uint32_t sub = fbits((float)mag * 2.98023223876953125e-8f);
+    const uint32_t sub = fbits(fmaf(bitsf(nrm), 2.0f, -6.103515625e-05f));
     return bitsf(sign | (mag >= 0x0800u ? nrm : sub));
 }
 
@@ -224,22 +239,23 @@ template <int FT> struct Ddf;
 template <> struct Ddf<ION_FP32> {
     using T = float;
     __device__ __forceinline__ static float dec(float v) { return v; }
+    __device__ __forceinline__ static float enc(float x) { return x; }
     __device__ __forceinline__ static float ld(const float* p, size_t i) { return p[i]; }
     __device__ __forceinline__ static void st(float* p, size_t i, float x) { p[i] = x; }
 };
 template <> struct Ddf<ION_FP16S> {
     using T = uint16_t;
     __device__ __forceinline__ static float dec(uint16_t v) { return __half2float(__ushort_as_half(v)) * 3.0517578E-5f; }
+    __device__ __forceinline__ static uint16_t enc(float x) { return __half_as_ushort(__float2half_rn(x * 32768.0f)); }
     __device__ __forceinline__ static float ld(const uint16_t* p, size_t i) { return dec(p[i]); }
-    __device__ __forceinline__ static void st(uint16_t* p, size_t i, float x) {
-        p[i] = __half_as_ushort(__float2half_rn(x * 32768.0f));
-    }
+    __device__ __forceinline__ static void st(uint16_t* p, size_t i, float x) { p[i] = enc(x); }
 };
 template <> struct Ddf<ION_FP16C> {
     using T = uint16_t;
     __device__ __forceinline__ static float dec(uint16_t v) { return fp16c_decode(v); }
+    __device__ __forceinline__ static uint16_t enc(float x) { return fp16c_encode(x); }
     __device__ __forceinline__ static float ld(const uint16_t* p, size_t i) { return dec(p[i]); }
-    __device__ __forceinline__ static void st(uint16_t* p, size_t i, float x) { p[i] = fp16c_encode(x); }
+    __device__ __forceinline__ static void st(uint16_t* p, size_t i, float x) { p[i] = enc(x); }
 };
 
 // x / b rounded to nearest, for finite b > 0, from y = RN(1/b) (__frcp_rn):

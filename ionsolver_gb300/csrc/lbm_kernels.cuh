@@ -125,15 +125,34 @@ __device__ __forceinline__ void ep_load(const typename D::T* f, uint32_t N, uint
         v[i + 1] = D::ld(f, (size_t)(odd ? i + 1 : i) * N + j(i));
     }
 }
-// IX: the type the slot offsets are computed in (uint32_t where Q N < 2^32 is known)
-template <class D, int Q, class NB, class IX = size_t>
-__device__ __forceinline__ void ep_store(typename D::T* f, uint32_t N, uint32_t n, bool odd, const NB& j, const float* v) {
-    D::st(f, n, v[0]);
+// Where a cell's new DDFs go (Esoteric-Pull, sim_kernels.cl:397-410): DDF 0 to slot
+// 0 of the cell (st0), the DDF of odd direction i to slot odd ? i + 1 : i of the
+// neighbour in direction i (st_nbr), that of direction i + 1 to slot odd ? i : i + 1
+// of the cell (st_own) -- exactly the locations the cell read its DDFs from.
+// GlobalDst computes the addresses; IX is the type the slot offsets are computed in
+// (uint32_t where Q N < 2^32 is known).
+template <class D, class NB, class IX = size_t>
+struct GlobalDst {
+    typename D::T* f;
+    uint32_t N, n;
+    bool odd;
+    const NB& j;
+    __device__ __forceinline__ void st0(float v) const { D::st(f, n, v); }
+    __device__ __forceinline__ void st_nbr(int i, float v) const { D::st(f, (IX)(odd ? i + 1 : i) * N + j(i), v); }
+    __device__ __forceinline__ void st_own(int i, float v) const { D::st(f, (IX)(odd ? i : i + 1) * N + n, v); }
+};
+template <int Q, class DST>
+__device__ __forceinline__ void ep_store_to(const DST& o, const float* v) {
+    o.st0(v[0]);
 #pragma unroll
     for (int i = 1; i < Q; i += 2) {
-        D::st(f, (IX)(odd ? i + 1 : i) * N + j(i), v[i]);
-        D::st(f, (IX)(odd ? i : i + 1) * N + n, v[i + 1]);
+        o.st_nbr(i, v[i]);
+        o.st_own(i, v[i + 1]);
     }
+}
+template <class D, int Q, class NB, class IX = size_t>
+__device__ __forceinline__ void ep_store(typename D::T* f, uint32_t N, uint32_t n, bool odd, const NB& j, const float* v) {
+    ep_store_to<Q>(GlobalDst<D, NB, IX>{f, N, n, odd, j}, v);
 }
 
 // L2 prefetch of the slots ep_load will read (no registers held; the later
@@ -176,32 +195,67 @@ struct GlobalSrc {
                                          float* v, int) const {
         ep_load<D, Q>(f, N, n, odd, j, v);
     }
+    template <class D, int Q, class IX, class NB>
+    __device__ __forceinline__ GlobalDst<D, NB, IX> dst(typename D::T* f, uint32_t N, uint32_t n, bool odd, const NB& j,
+                                                        int) const {
+        return {f, N, n, odd, j};
+    }
 };
 // D3Q19 offsets (in rows) of the staged streams of each lattice: fi 19, ei 19, fqi 7
 __host__ __device__ constexpr uint32_t row_stream_base(int lat) { return lat == LAT_FI ? 0u : lat == LAT_EI ? 19u : 38u; }
-// From one x-row staged in shared memory by k_sc_rows: stream s of a lattice holds
-// the row that DDF s of every cell of the row is read from (stream 0 and the odd
-// streams: the cell's own row; stream i + 1: the row of the neighbour in direction i,
-// read at the neighbour's x), then the E/B rows and the flags row.
-template <class T>
+// x shift of the neighbour row read for direction i (i odd) of a D3Q19 or D3Q7 lattice
+template <int Q>
+__host__ __device__ constexpr int row_cx(int i) { return Q == 7 ? (i == 1 ? 1 : 0) : VSet<19>::c(i, 0); }
+
+// A cell's new DDFs into the staged row they were read from (the cell's stores land
+// exactly on its loads, see GlobalDst): stream i at x for st_own, stream i + 1 at the
+// x of the neighbour for st_nbr.  RS: the row stride in elements (0: nx).
+template <class D, int Q, uint32_t RS>
+struct RowDst {
+    typename D::T* r;  // the lattice's stream 0
+    uint32_t nx, x, xp, xm;
+    __device__ __forceinline__ uint32_t stride() const { return RS ? RS : nx; }
+    __device__ __forceinline__ void st0(float v) const { r[x] = D::enc(v); }
+    __device__ __forceinline__ void st_own(int i, float v) const { r[(uint32_t)i * stride() + x] = D::enc(v); }
+    __device__ __forceinline__ void st_nbr(int i, float v) const {
+        const int cx = row_cx<Q>(i);
+        r[(uint32_t)(i + 1) * stride() + (cx > 0 ? xp : cx < 0 ? xm : x)] = D::enc(v);
+    }
+};
+
+// From one x-row staged in shared memory by the row kernels: stream s of a lattice
+// holds the row that DDF s of every cell of the row is read from (stream 0 and the
+// odd streams: the cell's own row; stream i + 1: the row of the neighbour in direction
+// i, read at the neighbour's x), then the E/B rows and the flags row.  RS: the row
+// stride in elements (0: nx).  WB: the new DDFs are written back into the staged rows
+// (the kernel then copies the rows back to global memory) instead of to global memory.
+template <class T, uint32_t RS = 0, bool WB = false>
 struct RowSrc {
     static constexpr bool prefetch = false;
-    const uint8_t* buf;
+    uint8_t* buf;
     uint32_t nx, x, xp, xm, eb_off, fl_off;
+    __device__ __forceinline__ uint32_t stride() const { return RS ? RS : nx; }
     __device__ __forceinline__ uint8_t flags(const DevLbm&, uint32_t) const { return buf[fl_off + x]; }
     __device__ __forceinline__ float eb(const DevLbm&, int c, uint32_t) const {
-        return reinterpret_cast<const float*>(buf + eb_off)[(uint32_t)c * nx + x];
+        return reinterpret_cast<const float*>(buf + eb_off)[(uint32_t)c * stride() + x];
     }
     template <class D, int Q, class NB>
     __device__ __forceinline__ void load(const T*, uint32_t, uint32_t, bool, const NB&, float* v, int lat) const {
-        const T* r = reinterpret_cast<const T*>(buf) + row_stream_base(lat) * nx;
+        const T* r = reinterpret_cast<const T*>(buf) + row_stream_base(lat) * stride();
         v[0] = D::dec(r[x]);
 #pragma unroll
         for (int i = 1; i < Q; i += 2) {
-            const int cx = Q == 7 ? (i == 1 ? 1 : 0) : VSet<19>::c(i, 0);
-            v[i] = D::dec(r[(uint32_t)i * nx + x]);
-            v[i + 1] = D::dec(r[(uint32_t)(i + 1) * nx + (cx > 0 ? xp : cx < 0 ? xm : x)]);
+            const int cx = row_cx<Q>(i);
+            v[i] = D::dec(r[(uint32_t)i * stride() + x]);
+            v[i + 1] = D::dec(r[(uint32_t)(i + 1) * stride() + (cx > 0 ? xp : cx < 0 ? xm : x)]);
         }
+    }
+    template <class D, int Q, class IX, class NB>
+    __device__ __forceinline__ auto dst(typename D::T* f, uint32_t N, uint32_t n, bool odd, const NB& j, int lat) const {
+        if constexpr (WB)
+            return RowDst<D, Q, RS>{reinterpret_cast<T*>(buf) + row_stream_base(lat) * stride(), nx, x, xp, xm};
+        else
+            return GlobalDst<D, NB, IX>{f, N, n, odd, j};
     }
 };
 
@@ -252,14 +306,13 @@ __device__ __forceinline__ float force_dir(const ForceState& s, int i) {
 
 // SRT collision + Esoteric-Pull store (sim_kernels.cl:714-723 / 649-656).
 // force: 0 = none (Fin = 0), 1 = Guo terms scaled by c_tau.
-template <class V, class D, class NB, class IX = size_t>
-__device__ __forceinline__ void srt_store(typename D::T* f, uint32_t N, uint32_t n, bool odd, const NB& j, const float* fh,
-                                          const EqState& es, const ForceState& fs, bool force, float c_tau, float w,
-                                          bool eqc) {
+template <class V, class DST>
+__device__ __forceinline__ void srt_store(const DST& o, const float* fh, const EqState& es, const ForceState& fs,
+                                          bool force, float c_tau, float w, bool eqc) {
     {
         const float feq = eq_zero<V>(es);
         const float F = force ? force_dir<V>(fs, 0) * c_tau : 0.0f;
-        D::st(f, n, eqc ? feq : fmaf(1.0f - w, fh[0], fmaf(w, feq, F)));
+        o.st0(eqc ? feq : fmaf(1.0f - w, fh[0], fmaf(w, feq, F)));
     }
 #pragma unroll
     for (int i = 1; i < V::q; i += 2) {
@@ -269,15 +322,15 @@ __device__ __forceinline__ void srt_store(typename D::T* f, uint32_t N, uint32_t
         const float Fb = force ? force_dir<V>(fs, i + 1) * c_tau : 0.0f;
         const float va = eqc ? fa : fmaf(1.0f - w, fh[i], fmaf(w, fa, Fa));
         const float vb = eqc ? fb : fmaf(1.0f - w, fh[i + 1], fmaf(w, fb, Fb));
-        D::st(f, (IX)(odd ? i + 1 : i) * N + j(i), va);
-        D::st(f, (IX)(odd ? i : i + 1) * N + n, vb);
+        o.st_nbr(i, va);
+        o.st_own(i, vb);
     }
 }
 
 // TRT collision + store (sim_kernels.cl:725-754)
-template <class V, class D, class NB, class IX = size_t>
-__device__ __forceinline__ void trt_store(typename D::T* f, uint32_t N, uint32_t n, bool odd, const NB& j, const float* fh,
-                                          const EqState& es, const ForceState& fs, bool force, float w, bool eqc) {
+template <class V, class DST>
+__device__ __forceinline__ void trt_store(const DST& o, const float* fh, const EqState& es, const ForceState& fs,
+                                          bool force, float w, bool eqc) {
     const float wp = w, wm = 1.0f / (0.1875f / (1.0f / w - 0.5f) + 0.5f);
     const float ctp = fmaf(wp, -0.25f, 0.5f), ctm = fmaf(wm, -0.25f, 0.5f);
     {
@@ -289,7 +342,7 @@ __device__ __forceinline__ void trt_store(typename D::T* f, uint32_t N, uint32_t
         }
         const float sym = ((feq - fh[0]) + feq) - fh[0];
         const float asym = ((feq - feq) - fh[0]) + fh[0];
-        D::st(f, n, eqc ? feq : fmaf(0.5f * wp, sym, fmaf(0.5f * wm, asym, fh[0] + F)));
+        o.st0(eqc ? feq : fmaf(0.5f * wp, sym, fmaf(0.5f * wm, asym, fh[0] + F)));
     }
 #pragma unroll
     for (int i = 1; i < V::q; i += 2) {
@@ -304,8 +357,8 @@ __device__ __forceinline__ void trt_store(typename D::T* f, uint32_t N, uint32_t
         const float ha = fh[i], hb = fh[i + 1];
         const float va = eqc ? ea : fmaf(0.5f * wp, ((ea - ha) + eb) - hb, fmaf(0.5f * wm, ((ea - eb) - ha) + hb, ha + Fa));
         const float vb = eqc ? eb : fmaf(0.5f * wp, ((eb - hb) + ea) - ha, fmaf(0.5f * wm, ((eb - ea) - hb) + ha, hb + Fb));
-        D::st(f, (IX)(odd ? i + 1 : i) * N + j(i), va);
-        D::st(f, (IX)(odd ? i : i + 1) * N + n, vb);
+        o.st_nbr(i, va);
+        o.st_own(i, vb);
     }
 }
 
@@ -324,33 +377,46 @@ __device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const
     using D = Ddf<FT>;
     using T = typename D::T;
     const uint32_t N = L.n;
-    {
-        const uint8_t fbo = S.flags(L, n) & F_BO;
-        if (fbo == F_S) return;
-        const bool eqc = L.ext_eq && fbo == F_E;
-        uint32_t x, y, z;
-        cell_xyz(L, n, x, y, z);
-        const Nbr nb(L, x, y, z);
-        const NbV<V> j{nb};
-        const float w = L.w;
-        const float c_tau = fmaf(w, -0.5f, 1.0f);
-        // MHD: the electron gas first -- it reads no value of the gas lattice, so
-        // its DDFs are dead before the gas DDFs are loaded (same values, fewer
-        // registers live at once)
-        float rhoe = 0.0f, Bx = 0.0f, By = 0.0f, Bz = 0.0f, Ex = 0.0f, Ey = 0.0f, Ez = 0.0f, dq_ecr = 0.0f;
-        if constexpr (MHD) {
-            // the gas and charge lattices are read after the electron gas: start them towards L2
-            if constexpr (SRC::prefetch) {
-                ep_prefetch<T, Q>((const T*)L.fi, N, n, odd, j);
-                ep_prefetch<T, 7>((const T*)L.fqi, N, n, odd, Nb7{nb});
-            }
-            Bx = S.eb(L, 0, n); By = S.eb(L, 1, n); Bz = S.eb(L, 2, n);
-            Ex = S.eb(L, 3, n); Ey = S.eb(L, 4, n); Ez = S.eb(L, 5, n);
-            // electron gas: moments, Lorentz force, Guo half-step, SRT, store
-            float ehn[Q];
-            S.template load<D, Q>((const T*)L.ei, N, n, odd, j, ehn, LAT_EI);
-            float uxe, uye, uze;
-            moments<V>(ehn, rhoe, uxe, uye, uze);
+    const uint8_t fbo = S.flags(L, n) & F_BO;
+    if (fbo == F_S) return;
+    const bool eqc = L.ext_eq && fbo == F_E;
+    uint32_t x, y, z;
+    cell_xyz(L, n, x, y, z);
+    const Nbr nb(L, x, y, z);
+    const NbV<V> j{nb};
+    const float w = L.w;
+    const float c_tau = fmaf(w, -0.5f, 1.0f);
+    float rhoe = 0.0f, Bx = 0.0f, By = 0.0f, Bz = 0.0f, Ex = 0.0f, Ey = 0.0f, Ez = 0.0f, dq_ecr = 0.0f;
+    if constexpr (MHD) {
+        // the gas and charge lattices are read after the electron gas: start them towards L2
+        if constexpr (SRC::prefetch) {
+            ep_prefetch<T, Q>((const T*)L.fi, N, n, odd, j);
+            ep_prefetch<T, 7>((const T*)L.fqi, N, n, odd, Nb7{nb});
+        }
+        Bx = S.eb(L, 0, n); By = S.eb(L, 1, n); Bz = S.eb(L, 2, n);
+        Ex = S.eb(L, 3, n); Ey = S.eb(L, 4, n); Ez = S.eb(L, 5, n);
+    }
+    // MHD: the electron gas first (pass 0), then the gas (pass 1).  The electron gas
+    // reads no value of the gas lattice, so its DDFs are dead before the gas DDFs load
+    // (fewer registers live at once).  With FP16C storage both passes run one copy of the
+    // load, moments, collision and store code (the loop is not unrolled): the integer
+    // codec makes the unrolled cell too large for the instruction cache, and sharing
+    // measured 11% faster at 256^3; FP32 and FP16S keep the unrolled form (the shared
+    // one measured equal and 2.5% slower).  Each pass computes exactly the values of
+    // the reference's code for its lattice.
+#pragma unroll(FT == ION_FP16C ? 1 : 2)
+    for (int pass = MHD ? 0 : 1; pass < 2; pass++) {
+        const bool electrons = MHD && pass == 0;
+        T* const f = (T*)(electrons ? L.ei : L.fi);
+        const int lat = electrons ? LAT_EI : LAT_FI;
+        float fh[Q];
+        S.template load<D, Q>(f, N, n, odd, j, fh, lat);
+        float rho, ux, uy, uz, fx, fy, fz;
+        bool force;
+        if (!electrons && eqc) { rho = L.rho[n]; ux = L.u[n]; uy = L.u[(size_t)N + n]; uz = L.u[2 * (size_t)N + n]; }
+        else moments<V>(fh, rho, ux, uy, uz);
+        if (electrons) {
+            // electron gas: Lorentz force, Guo half-step (sim_kernels.cl:530-656)
             if constexpr (ECR) {  // SUBGRID_ECR, sim_kernels.cl:564-628 (the ionisation term is the reference's placeholder)
                 const Nb7 j7{nb};
                 float ethn[7];
@@ -365,7 +431,7 @@ __device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const
                 const float kpar = ((Evx * Bx + Evy * By) + Evz * Bz) / (lB * lB);
                 const float pex = Evx - kpar * Bx, pey = Evy - kpar * By, pez = Evz - kpar * Bz;
                 const float Emag = sqrtf((pex * pex + pey * pey) + pez * pez);
-                Etn = Etn + (((L.keabs / L.kkbme) * (rhoe + 0.00001f)) / L.kkge) * (Emag * Emag);
+                Etn = Etn + (((L.keabs / L.kkbme) * (rho + 0.00001f)) / L.kkge) * (Emag * Emag);
                 // guiding-centre drift along -grad |B|
                 float gx = 0.0f, gy = 0.0f, gz = 0.0f;
                 if (!(x == 0u || x == L.nx - 1u || y == 0u || y == L.ny - 1u || z == 0u || z == L.nz - 1u)) {
@@ -376,88 +442,82 @@ __device__ __forceinline__ void sc_cell(const DevLbm& L, const uint32_t n, const
                 }
                 const float kt = L.kkbme * Etn;
                 const float dux = (kt * gx) / lB, duy = (kt * gy) / lB, duz = (kt * gz) / lB;
-                uxe = uxe + dux;
-                uye = uye + duy;
-                uze = uze + duz;
+                ux = ux + dux;
+                uy = uy + duy;
+                uz = uz + duz;
                 Etn = Etn - sqrtf((dux * dux + duy * duy) + duz * duz) / L.kkbme;
                 float eteq[7];
-                adv_equilibrium(Etn, uxe, uye, uze, eteq);
+                adv_equilibrium(Etn, ux, uy, uz, eteq);
                 if (L.update_fields) L.et[n] = Etn;
 #pragma unroll
                 for (int i = 0; i < 7; i++) ethn[i] = fmaf(1.0f - L.wq, ethn[i], L.wq * eteq[i]);
                 ep_store<D, 7>((T*)L.eti, N, n, odd, j7, ethn);
                 dq_ecr = 0.0001f * Etn;  // ionisation: added to the electron and the gas charge
-                rhoe = rhoe + dq_ecr;
+                rho = rho + dq_ecr;
             }
-            const float cxv = uye * Bz - uze * By, cyv = uze * Bx - uxe * Bz, czv = uxe * By - uye * Bx;
-            const float nre = -rhoe;
-            const float efx = nre * (Ex + cxv), efy = nre * (Ey + cyv), efz = nre * (Ez + czv);
-            const float r2e = 0.5f / (rhoe * L.kkge);
-            uxe = clampf(fmaf(efx, r2e, uxe), -CS, CS);
-            uye = clampf(fmaf(efy, r2e, uye), -CS, CS);
-            uze = clampf(fmaf(efz, r2e, uze), -CS, CS);
-            const ForceState fe = force_state<V>(uxe, uye, uze, efx, efy, efz);
-            const EqState ee = eq_state(rhoe, uxe, uye, uze);
-            srt_store<V, D, NbV<V>, IX>((T*)L.ei, N, n, odd, j, ehn, ee, fe, true, c_tau, w, eqc);
-        }
-        float fhn[Q];
-        S.template load<D, Q>((const T*)L.fi, N, n, odd, j, fhn, LAT_FI);
-        float rhon, uxn, uyn, uzn;
-        if (eqc) { rhon = L.rho[n]; uxn = L.u[n]; uyn = L.u[(size_t)N + n]; uzn = L.u[2 * (size_t)N + n]; }
-        else moments<V>(fhn, rhon, uxn, uyn, uzn);
-
-        float fxn = L.fx, fyn = L.fy, fzn = L.fz;
-        if (L.ext_ff) { fxn = fxn + L.F[n]; fyn = fyn + L.F[(size_t)N + n]; fzn = fzn + L.F[2 * (size_t)N + n]; }
-
-        if constexpr (MHD) {
-            // charge advection (D3Q7): load, charge, collide, store
-            const Nb7 j7{nb};
-            float rhoq;
-            {
-                float qhn[7];
-                S.template load<D, 7>((const T*)L.fqi, N, n, odd, j7, qhn, LAT_FQI);
-                rhoq = 0.0f;
-#pragma unroll
-                for (int i = 0; i < 7; i++) rhoq = rhoq + qhn[i];
-                rhoq = rhoq + 1.0f;
-                if constexpr (ECR) rhoq = rhoq + dq_ecr;
-                float aeq[7];
-                adv_equilibrium(rhoq, uxn, uyn, uzn, aeq);
-#pragma unroll
-                for (int i = 0; i < 7; i++) qhn[i] = fmaf(1.0f - L.wq, qhn[i], L.wq * aeq[i]);
-                ep_store<D, 7, Nb7, IX>((T*)L.fqi, N, n, odd, j7, qhn);
-            }
-            L.q[n] = rhoq - rhoe;
-            // Lorentz force on the gas
-            fxn = fxn + rhoq * ((Ex + uyn * Bz) - uzn * By);
-            fyn = fyn + rhoq * ((Ey + uzn * Bx) - uxn * Bz);
-            fzn = fzn + rhoq * ((Ez + uxn * By) - uyn * Bx);
-            // LOD contribution: velocity / bin volume (the charge is q[n])
-            if (L.depth > 0u) {
-                L.lod_cell[n] = uxn * L.ils;
-                L.lod_cell[(size_t)N + n] = uyn * L.ils;
-                L.lod_cell[2 * (size_t)N + n] = uzn * L.ils;
-            }
-        }
-
-        if (L.ext_vf) {
-            const float r2 = 0.5f / rhon;
-            uxn = clampf(fmaf(fxn, r2, uxn), -CS, CS);
-            uyn = clampf(fmaf(fyn, r2, uyn), -CS, CS);
-            uzn = clampf(fmaf(fzn, r2, uzn), -CS, CS);
+            const float cxv = uy * Bz - uz * By, cyv = uz * Bx - ux * Bz, czv = ux * By - uy * Bx;
+            const float nre = -rho;
+            fx = nre * (Ex + cxv); fy = nre * (Ey + cyv); fz = nre * (Ez + czv);
+            const float r2e = 0.5f / (rho * L.kkge);
+            ux = clampf(fmaf(fx, r2e, ux), -CS, CS);
+            uy = clampf(fmaf(fy, r2e, uy), -CS, CS);
+            uz = clampf(fmaf(fz, r2e, uz), -CS, CS);
+            rhoe = rho;
+            force = true;
         } else {
-            uxn = clampf(uxn, -CS, CS);
-            uyn = clampf(uyn, -CS, CS);
-            uzn = clampf(uzn, -CS, CS);
+            fx = L.fx; fy = L.fy; fz = L.fz;
+            if (L.ext_ff) { fx = fx + L.F[n]; fy = fy + L.F[(size_t)N + n]; fz = fz + L.F[2 * (size_t)N + n]; }
+            if constexpr (MHD) {
+                // charge advection (D3Q7): load, charge, collide, store
+                const Nb7 j7{nb};
+                float rhoq;
+                {
+                    float qhn[7];
+                    S.template load<D, 7>((const T*)L.fqi, N, n, odd, j7, qhn, LAT_FQI);
+                    rhoq = 0.0f;
+#pragma unroll
+                    for (int i = 0; i < 7; i++) rhoq = rhoq + qhn[i];
+                    rhoq = rhoq + 1.0f;
+                    if constexpr (ECR) rhoq = rhoq + dq_ecr;
+                    float aeq[7];
+                    adv_equilibrium(rhoq, ux, uy, uz, aeq);
+#pragma unroll
+                    for (int i = 0; i < 7; i++) qhn[i] = fmaf(1.0f - L.wq, qhn[i], L.wq * aeq[i]);
+                    ep_store_to<7>(S.template dst<D, 7, IX>((T*)L.fqi, N, n, odd, j7, LAT_FQI), qhn);
+                }
+                L.q[n] = rhoq - rhoe;
+                // Lorentz force on the gas
+                fx = fx + rhoq * ((Ex + uy * Bz) - uz * By);
+                fy = fy + rhoq * ((Ey + uz * Bx) - ux * Bz);
+                fz = fz + rhoq * ((Ez + ux * By) - uy * Bx);
+                // LOD contribution: velocity / bin volume (the charge is q[n])
+                if (L.depth > 0u) {
+                    L.lod_cell[n] = ux * L.ils;
+                    L.lod_cell[(size_t)N + n] = uy * L.ils;
+                    L.lod_cell[2 * (size_t)N + n] = uz * L.ils;
+                }
+            }
+            if (L.ext_vf) {
+                const float r2 = 0.5f / rho;
+                ux = clampf(fmaf(fx, r2, ux), -CS, CS);
+                uy = clampf(fmaf(fy, r2, uy), -CS, CS);
+                uz = clampf(fmaf(fz, r2, uz), -CS, CS);
+            } else {
+                ux = clampf(ux, -CS, CS);
+                uy = clampf(uy, -CS, CS);
+                uz = clampf(uz, -CS, CS);
+            }
+            if (L.update_fields && !eqc) {
+                L.rho[n] = rho;
+                L.u[n] = ux; L.u[(size_t)N + n] = uy; L.u[2 * (size_t)N + n] = uz;
+            }
+            force = L.ext_vf;
         }
-        if (L.update_fields && !eqc) {
-            L.rho[n] = rhon;
-            L.u[n] = uxn; L.u[(size_t)N + n] = uyn; L.u[2 * (size_t)N + n] = uzn;
-        }
-        const EqState es = eq_state(rhon, uxn, uyn, uzn);
-        const ForceState fs = force_state<V>(uxn, uyn, uzn, fxn, fyn, fzn);
-        if constexpr (TRT) trt_store<V, D, NbV<V>, IX>((T*)L.fi, N, n, odd, j, fhn, es, fs, L.ext_vf, w, eqc);
-        else srt_store<V, D, NbV<V>, IX>((T*)L.fi, N, n, odd, j, fhn, es, fs, L.ext_vf, c_tau, w, eqc);
+        const EqState es = eq_state(rho, ux, uy, uz);
+        const ForceState fs = force_state<V>(ux, uy, uz, fx, fy, fz);
+        const auto dst = S.template dst<D, Q, IX>(f, N, n, odd, j, lat);
+        if (TRT && !electrons) trt_store<V>(dst, fh, es, fs, force, w, eqc);
+        else srt_store<V>(dst, fh, es, fs, force, c_tau, w, eqc);
     }
 }
 
@@ -479,12 +539,15 @@ __global__ void __launch_bounds__(256, MHD ? 2 : 4) k_stream_collide(const DevLb
 // buffer.  All streams are contiguous rows, so the copies keep tens of KB per SM in
 // flight without holding registers.  In Esoteric-Pull every slot is read and
 // written by the same cell within a step, so staging a row ahead of its cells'
-// stores is safe.  The arithmetic is sc_cell's (RowSrc only changes where values
-// are read); stores go to global memory as before.  Two forms: k_sc_rows_ws (rows
-// of up to 256 cells: a producer warp and "full"/"empty" mbarriers, no CTA-wide
-// barrier per row) and k_sc_rows (longer rows: thread 0 stages, a CTA barrier
-// releases the buffer).  A copy that does not land within the wait limit sets
-// *err and the CTA stops after waiting (bounded) for its copies in flight.
+// stores is safe, and the cells' new DDFs can go back into the staged rows (RowDst):
+// once a row is computed, its lattice streams are copied back to their global rows
+// with cp.async.bulk (shared -> global), whole rows instead of one 2- or 4-byte store
+// per DDF.  The arithmetic is sc_cell's (RowSrc/RowDst only change where values are
+// read and written).  Two forms: k_sc_rows_ws (rows of up to 256 cells: a producer
+// warp and "full"/"empty" mbarriers, no CTA-wide barrier per row) and k_sc_rows
+// (longer rows: thread 0 stages and writes back, a CTA barrier releases the buffer).
+// A copy that does not land within the wait limit sets *err and the CTA stops after
+// waiting (bounded) for its copies in flight; rows not computed are not written back.
 // ---------------------------------------------------------------------------
 template <int FT, bool MHD>
 __host__ __device__ constexpr uint32_t row_streams() { return MHD ? 45u : 19u; }
@@ -495,18 +558,53 @@ __host__ __device__ inline uint32_t row_bytes(uint32_t nx) {
     return row_streams<FT, MHD>() * nx * (uint32_t)sizeof(T) + (MHD ? 6u * nx * 4u : 0u) + ((nx + 15u) & ~15u);
 }
 
-// Rows longer than 256 cells: CTAs of at most 256 threads, each thread two cells of
-// the row; thread 0 stages the next row at the start of each row and a CTA barrier
-// releases a buffer (measured faster than the producer-warp form at 384 cells, where
-// two cells per thread want the registers the extra warp would take).
+// The global rows of the lattice streams of row r = (y, z), in staging-buffer order:
+// op(stream, pointer to the row's first element) for each lattice (gas, then electron
+// gas and charge), stream 0 and the odd streams from the own row, stream i + 1 from the
+// row of the neighbour in direction i (periodic in y and z).
+template <int FT, bool MHD, class OP>
+__device__ __forceinline__ void for_row_streams(const DevLbm& L, uint32_t r, bool odd, OP&& op) {
+    using V = VSet<19>;
+    using T = typename Ddf<FT>::T;
+    const uint32_t nx = L.nx, ny = L.ny, nz = L.nz, N = L.n;
+    const uint32_t y = r % ny, z = r / ny, own = (y + z * ny) * nx;
+    auto lattice = [&](T* f, uint32_t base, int Q) {
+        op(base, f + own);
+        for (int i = 1; i < Q; i += 2) {
+            const int cy = Q == 7 ? (i == 3 ? 1 : 0) : V::c(i, 1), cz = Q == 7 ? (i == 5 ? 1 : 0) : V::c(i, 2);
+            const uint32_t yy = cy > 0 ? (y + 1u == ny ? 0u : y + 1u) : cy < 0 ? (y == 0u ? ny - 1u : y - 1u) : y;
+            const uint32_t zz = cz > 0 ? (z + 1u == nz ? 0u : z + 1u) : cz < 0 ? (z == 0u ? nz - 1u : z - 1u) : z;
+            const uint32_t s_own = odd ? (uint32_t)i : (uint32_t)i + 1u, s_nbr = odd ? (uint32_t)i + 1u : (uint32_t)i;
+            op(base + i, f + (size_t)s_own * N + own);
+            op(base + i + 1, f + (size_t)s_nbr * N + (yy + zz * ny) * nx);
+        }
+    };
+    lattice((T*)L.fi, row_stream_base(LAT_FI), 19);
+    if constexpr (MHD) {
+        lattice((T*)L.ei, row_stream_base(LAT_EI), 19);
+        lattice((T*)L.fqi, row_stream_base(LAT_FQI), 7);
+    }
+}
+
+__device__ __forceinline__ void bulk_s2g(void* dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)), "r"(bytes)
+                 : "memory");
+}
+
+// Rows longer than 384 cells: CTAs of at most 256 threads, each thread two or more
+// cells of the row; thread 0 stages the next row at the start of each row and a CTA
+// barrier releases a buffer.  The new DDFs
+// are stored to global memory directly: writing them back through the staged rows,
+// as k_sc_rows_ws does, measured slower here (FP16S MHD at 384^3 3.60 -> 4.09 ms, FP32
+// MHD at 288^3 2.62 -> 3.54 ms, one CTA per SM), because thread 0 then has to wait
+// for the copy-back to read a buffer before it can stage the next row into it.
 template <int FT, bool MHD, bool TRT>
 __global__ void __launch_bounds__(256, 2) k_sc_rows(const DevLbm L, const uint32_t odd_t, uint32_t* err) {
-    using V = VSet<19>;
     using T = typename Ddf<FT>::T;
     extern __shared__ __align__(128) uint8_t rows_smem[];
     __shared__ __align__(8) uint64_t bar[2];
     const bool odd = odd_t != 0u;
-    const uint32_t nx = L.nx, ny = L.ny, nz = L.nz, nrows = ny * nz, N = L.n;
+    const uint32_t nx = L.nx, ny = L.ny, nrows = ny * L.nz, N = L.n;
     const uint32_t rb = nx * (uint32_t)sizeof(T), RB = row_bytes<FT, MHD>(nx);
     const uint32_t eb_off = row_streams<FT, MHD>() * rb, fl_off = eb_off + (MHD ? 6u * nx * 4u : 0u);
     if (threadIdx.x == 0) {
@@ -518,24 +616,10 @@ __global__ void __launch_bounds__(256, 2) k_sc_rows(const DevLbm L, const uint32
     // copies of row r into buffer b (one thread)
     auto stage = [&](uint32_t r, uint32_t b) {
         uint8_t* dst = rows_smem + b * RB;
-        const uint32_t y = r % ny, z = r / ny;
-        const uint32_t own = (y + z * ny) * nx;
+        const uint32_t own = r * nx;
         mbar_expect_tx(&bar[b], RB);
-        auto lattice = [&](const T* f, uint32_t base, int Q) {
-            bulk_g2s(dst + base * rb, f + own, rb, &bar[b]);
-            for (int i = 1; i < Q; i += 2) {
-                const int cy = Q == 7 ? (i == 3 ? 1 : 0) : V::c(i, 1), cz = Q == 7 ? (i == 5 ? 1 : 0) : V::c(i, 2);
-                const uint32_t yy = cy > 0 ? (y + 1u == ny ? 0u : y + 1u) : cy < 0 ? (y == 0u ? ny - 1u : y - 1u) : y;
-                const uint32_t zz = cz > 0 ? (z + 1u == nz ? 0u : z + 1u) : cz < 0 ? (z == 0u ? nz - 1u : z - 1u) : z;
-                const uint32_t s_own = odd ? (uint32_t)i : (uint32_t)i + 1u, s_nbr = odd ? (uint32_t)i + 1u : (uint32_t)i;
-                bulk_g2s(dst + (base + i) * rb, f + (size_t)s_own * N + own, rb, &bar[b]);
-                bulk_g2s(dst + (base + i + 1) * rb, f + (size_t)s_nbr * N + (yy + zz * ny) * nx, rb, &bar[b]);
-            }
-        };
-        lattice((const T*)L.fi, row_stream_base(LAT_FI), 19);
+        for_row_streams<FT, MHD>(L, r, odd, [&](uint32_t st, T* g) { bulk_g2s(dst + st * rb, g, rb, &bar[b]); });
         if constexpr (MHD) {
-            lattice((const T*)L.ei, row_stream_base(LAT_EI), 19);
-            lattice((const T*)L.fqi, row_stream_base(LAT_FQI), 7);
             for (uint32_t c = 0; c < 3; c++) {
                 bulk_g2s(dst + eb_off + c * nx * 4u, L.b_dyn + (size_t)c * N + own, nx * 4u, &bar[b]);
                 bulk_g2s(dst + eb_off + (3u + c) * nx * 4u, L.e_dyn + (size_t)c * N + own, nx * 4u, &bar[b]);
@@ -552,7 +636,7 @@ __global__ void __launch_bounds__(256, 2) k_sc_rows(const DevLbm L, const uint32
         if (threadIdx.x == 0 && r + gridDim.x < nrows) stage(r + gridDim.x, b ^ 1u);
         ok = mbar_wait(&bar[b], (k >> 1) & 1u, L.wait_limit);
         if (!__syncthreads_and(ok)) break;
-        const uint8_t* buf = rows_smem + b * RB;
+        uint8_t* buf = rows_smem + b * RB;
         const uint32_t y = r % ny, z = r / ny;
         for (uint32_t x = threadIdx.x; x < nx; x += blockDim.x) {
             const RowSrc<T> S{buf, nx, x, x + 1u == nx ? 0u : x + 1u, x == 0u ? nx - 1u : x - 1u, eb_off, fl_off};
@@ -584,20 +668,44 @@ __device__ __forceinline__ bool mbar_wait_or_fail(uint64_t* bar, uint32_t parity
     return false;
 }
 
-// Rows of up to 256 cells: blockDim.x = compute threads + 32; the last warp stages rows,
-// the others compute (one cell per thread and row)
-template <int FT, bool MHD, bool TRT>
-__global__ void __launch_bounds__(288, MHD ? 2 : 3) k_sc_rows_ws(const DevLbm L, const uint32_t odd_t, uint32_t* err) {
-    using V = VSet<19>;
+// Rows of up to 384 cells (WS_ROW): blockDim.x = compute threads + 32.  The last warp
+// stages rows and writes them back; the others compute (one cell per thread and row).
+// The row buffer has a fixed stride of RS elements per stream (the smallest of 128, 256
+// and 384 that holds the row: a small buffer keeps more CTAs per SM), so every
+// shared-memory access of a cell is a register plus a constant offset.  The cells' new
+// DDFs go into the staged rows they were read from (RowDst), and the producer copies
+// each finished row's lattice streams back to their global rows with cp.async.bulk
+// (shared -> global): a row's streams are read and written by that row's cells only,
+// so no other CTA touches them within the step.  The other outputs (q, the LOD
+// velocity, rho, u) are stored directly.
+constexpr uint32_t WS_ROW = 384;
+__host__ __device__ constexpr uint32_t ws_stride(uint32_t nx) { return nx <= 128u ? 128u : nx <= 256u ? 256u : 384u; }
+template <int FT, bool MHD, uint32_t RS>
+__host__ __device__ constexpr uint32_t ws_row_bytes() {
+    return row_streams<FT, MHD>() * RS * (uint32_t)sizeof(typename Ddf<FT>::T) + (MHD ? 6u * RS * 4u : 0u) + RS;
+}
+
+// Rows of up to 256 cells: three CTAs of up to 288 threads per SM (72 registers; FP16
+// MHD rows of 256 cells then run 24 compute warps per SM instead of 16: 0.920 -> 0.845
+// ms at 256^3 FP16S), except MHD with TRT, which spills at 72 registers.  Rows of up to
+// 384 cells: two CTAs of up to 416 threads (78 registers), one for MHD with TRT.
+template <uint32_t RS>
+__host__ __device__ constexpr int ws_threads() { return RS == 384u ? 416 : 288; }
+template <uint32_t RS, bool MHD, bool TRT>
+__host__ __device__ constexpr int ws_min_ctas() { return RS == 384u ? ((MHD && TRT) ? 1 : 2) : ((MHD && TRT) ? 2 : 3); }
+template <int FT, bool MHD, bool TRT, uint32_t RS>
+__global__ void __launch_bounds__(ws_threads<RS>(), ws_min_ctas<RS, MHD, TRT>()) k_sc_rows_ws(const DevLbm L, const uint32_t odd_t, uint32_t* err) {
     using T = typename Ddf<FT>::T;
+    constexpr uint32_t RB = ws_row_bytes<FT, MHD, RS>();
+    constexpr uint32_t SB = RS * (uint32_t)sizeof(T);  // bytes per stream row
+    constexpr uint32_t eb_off = row_streams<FT, MHD>() * SB, fl_off = eb_off + (MHD ? 6u * RS * 4u : 0u);
     extern __shared__ __align__(128) uint8_t rows_smem[];
     __shared__ __align__(8) uint64_t full[2], empty[2];
     __shared__ uint32_t fail_flag, issued;  // rows the producer has staged
     volatile uint32_t* fail = &fail_flag;
     const bool odd = odd_t != 0u;
     const uint32_t nx = L.nx, ny = L.ny, nz = L.nz, nrows = ny * nz, N = L.n;
-    const uint32_t rb = nx * (uint32_t)sizeof(T), RB = row_bytes<FT, MHD>(nx);
-    const uint32_t eb_off = row_streams<FT, MHD>() * rb, fl_off = eb_off + (MHD ? 6u * nx * 4u : 0u);
+    const uint32_t rb = nx * (uint32_t)sizeof(T);  // bytes of one stream's row in global memory
     const uint32_t nct = blockDim.x - 32u, ncw = nct / 32u;  // compute threads and warps
     if (threadIdx.x == 0) {
         mbar_init(&full[0], 1u);
@@ -611,38 +719,46 @@ __global__ void __launch_bounds__(288, MHD ? 2 : 3) k_sc_rows_ws(const DevLbm L,
     __syncthreads();
     const uint32_t my_rows = blockIdx.x < nrows ? (nrows - 1u - blockIdx.x) / gridDim.x + 1u : 0u;
     if (threadIdx.x >= nct) {
-        // producer: row k of this CTA into buffer k & 1, once the compute warps released it
         if (threadIdx.x == nct) {
-            for (uint32_t k = 0; k < my_rows; k++) {
+            auto for_streams = [&](uint32_t r, auto&& op) { for_row_streams<FT, MHD>(L, r, odd, op); };
+            // row k of this CTA lives in buffer k & 1
+            auto write_back = [&](uint32_t k) {
+                const uint8_t* src = rows_smem + (k & 1u) * RB;
+                for_streams(blockIdx.x + k * gridDim.x, [&](uint32_t st, T* g) { bulk_s2g(g, src + st * SB, rb); });
+                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            };
+            uint32_t k = 0;
+            for (; k < my_rows; k++) {
                 const uint32_t b = k & 1u, r = blockIdx.x + k * gridDim.x;
-                if (k >= 2 && !mbar_wait_or_fail(&empty[b], ((k - 2) >> 1) & 1u, fail, L.wait_limit)) break;
+                if (k >= 2) {
+                    // row k - 2 computed: copy it back, and wait until the copies have read the buffer
+                    if (!mbar_wait_or_fail(&empty[b], ((k - 2) >> 1) & 1u, fail, L.wait_limit)) break;
+                    if (*fail) break;
+                    write_back(k - 2u);
+                    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                }
                 if (*fail) break;
                 uint8_t* dst = rows_smem + b * RB;
                 const uint32_t y = r % ny, z = r / ny, own = (y + z * ny) * nx;
-                mbar_expect_tx(&full[b], RB);
-                auto lattice = [&](const T* f, uint32_t base, int Q) {
-                    bulk_g2s(dst + base * rb, f + own, rb, &full[b]);
-                    for (int i = 1; i < Q; i += 2) {
-                        const int cy = Q == 7 ? (i == 3 ? 1 : 0) : V::c(i, 1), cz = Q == 7 ? (i == 5 ? 1 : 0) : V::c(i, 2);
-                        const uint32_t yy = cy > 0 ? (y + 1u == ny ? 0u : y + 1u) : cy < 0 ? (y == 0u ? ny - 1u : y - 1u) : y;
-                        const uint32_t zz = cz > 0 ? (z + 1u == nz ? 0u : z + 1u) : cz < 0 ? (z == 0u ? nz - 1u : z - 1u) : z;
-                        const uint32_t s_own = odd ? (uint32_t)i : (uint32_t)i + 1u, s_nbr = odd ? (uint32_t)i + 1u : (uint32_t)i;
-                        bulk_g2s(dst + (base + i) * rb, f + (size_t)s_own * N + own, rb, &full[b]);
-                        bulk_g2s(dst + (base + i + 1) * rb, f + (size_t)s_nbr * N + (yy + zz * ny) * nx, rb, &full[b]);
-                    }
-                };
-                lattice((const T*)L.fi, row_stream_base(LAT_FI), 19);
+                mbar_expect_tx(&full[b], row_streams<FT, MHD>() * rb + (MHD ? 6u * nx * 4u : 0u) + ((nx + 15u) & ~15u));
+                for_streams(r, [&](uint32_t st, T* g) { bulk_g2s(dst + st * SB, g, rb, &full[b]); });
                 if constexpr (MHD) {
-                    lattice((const T*)L.ei, row_stream_base(LAT_EI), 19);
-                    lattice((const T*)L.fqi, row_stream_base(LAT_FQI), 7);
                     for (uint32_t c = 0; c < 3; c++) {
-                        bulk_g2s(dst + eb_off + c * nx * 4u, L.b_dyn + (size_t)c * N + own, nx * 4u, &full[b]);
-                        bulk_g2s(dst + eb_off + (3u + c) * nx * 4u, L.e_dyn + (size_t)c * N + own, nx * 4u, &full[b]);
+                        bulk_g2s(dst + eb_off + c * RS * 4u, L.b_dyn + (size_t)c * N + own, nx * 4u, &full[b]);
+                        bulk_g2s(dst + eb_off + (3u + c) * RS * 4u, L.e_dyn + (size_t)c * N + own, nx * 4u, &full[b]);
                     }
                 }
                 bulk_g2s(dst + fl_off, L.flags + own, (nx + 15u) & ~15u, &full[b]);
                 issued = k + 1u;
             }
+            // the last (up to) two rows, once computed
+            if (k == my_rows) {
+                for (uint32_t t = my_rows > 2u ? my_rows - 2u : 0u; t < my_rows; t++) {
+                    if (!mbar_wait_or_fail(&empty[t & 1u], (t >> 1) & 1u, fail, L.wait_limit) || *fail) break;
+                    write_back(t);
+                }
+            }
+            asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
         }
         __syncwarp();
     } else {
@@ -651,12 +767,15 @@ __global__ void __launch_bounds__(288, MHD ? 2 : 3) k_sc_rows_ws(const DevLbm L,
             const uint32_t b = k & 1u, r = blockIdx.x + k * gridDim.x;
             const bool go = mbar_wait_or_fail(&full[b], (k >> 1) & 1u, fail, L.wait_limit) && *fail == 0u;
             if (go) {
-                const uint8_t* buf = rows_smem + b * RB;
+                uint8_t* buf = rows_smem + b * RB;
                 const uint32_t y = r % ny, z = r / ny;
                 for (uint32_t x = threadIdx.x; x < nx; x += nct) {
-                    const RowSrc<T> S{buf, nx, x, x + 1u == nx ? 0u : x + 1u, x == 0u ? nx - 1u : x - 1u, eb_off, fl_off};
-                    sc_cell<19, FT, MHD, TRT, false, RowSrc<T>, uint32_t>(L, x + (y + z * ny) * nx, odd, S);
+                    const RowSrc<T, RS, true> S{buf, nx, x, x + 1u == nx ? 0u : x + 1u, x == 0u ? nx - 1u : x - 1u,
+                                                 eb_off, fl_off};
+                    sc_cell<19, FT, MHD, TRT, false, RowSrc<T, RS, true>, uint32_t>(L, x + (y + z * ny) * nx, odd, S);
                 }
+                // the new DDFs (generic-proxy writes) become visible to the bulk copies
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             }
             __syncwarp();
             if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&empty[b])) : "memory");
@@ -677,19 +796,27 @@ __global__ void __launch_bounds__(288, MHD ? 2 : 3) k_sc_rows_ws(const DevLbm L,
 template <int FT, bool MHD, bool TRT>
 bool launch_sc_rows(const DevLbm& L, uint32_t o, uint32_t* err, cudaStream_t s) {
     // whole 16-byte rows, two buffers in shared memory, and 32-bit slot offsets (19 N < 2^32)
-    if (L.nx % 16u || 2u * row_bytes<FT, MHD>(L.nx) > 200u * 1024u || 19ull * L.n >= (1ull << 32)) return false;
-    const uint32_t smem = 2u * row_bytes<FT, MHD>(L.nx);
-    const bool ws = L.nx <= 256u;  // producer warp + one cell per thread and row
+    const bool ws = L.nx <= WS_ROW;  // producer warp + one cell per thread and row
+    const uint32_t rs = ws ? ws_stride(L.nx) : 0u;
+    static_assert(2u * ws_row_bytes<ION_FP32, true, WS_ROW>() <= 200u * 1024u, "two row buffers of the widest form");
+    const uint32_t smem = 2u * (rs == 128u   ? ws_row_bytes<FT, MHD, 128u>()
+                                : rs == 256u ? ws_row_bytes<FT, MHD, 256u>()
+                                : rs == 384u ? ws_row_bytes<FT, MHD, 384u>()
+                                             : row_bytes<FT, MHD>(L.nx));
+    if (L.nx % 16u || smem > 200u * 1024u || 19ull * L.n >= (1ull << 32)) return false;
     const uint32_t threads =
         ws ? (L.nx + 31u) / 32u * 32u + 32u : ((L.nx + ((L.nx + 255u) / 256u) - 1u) / ((L.nx + 255u) / 256u) + 31u) / 32u * 32u;
-    auto kern = ws ? k_sc_rows_ws<FT, MHD, TRT> : k_sc_rows<FT, MHD, TRT>;
+    auto kern = rs == 128u   ? k_sc_rows_ws<FT, MHD, TRT, 128u>
+                : rs == 256u ? k_sc_rows_ws<FT, MHD, TRT, 256u>
+                : rs == 384u ? k_sc_rows_ws<FT, MHD, TRT, 384u>
+                             : k_sc_rows<FT, MHD, TRT>;
     // the shared-memory opt-in and the occupancy of the last shape, per instantiation
     // (handles may step on several host threads)
     static std::mutex mu;
-    static bool attr[2] = {false, false};
-    static int per_sm_of[2] = {0, 0};
-    static uint32_t for_smem[2] = {0, 0}, for_threads[2] = {0, 0};
-    const int v = ws ? 1 : 0;
+    static bool attr[4] = {false, false, false, false};
+    static int per_sm_of[4] = {0, 0, 0, 0};
+    static uint32_t for_smem[4] = {0, 0, 0, 0}, for_threads[4] = {0, 0, 0, 0};
+    const int v = (int)(rs / 128u);
     int per_sm = 0;
     {
         std::lock_guard<std::mutex> lock(mu);

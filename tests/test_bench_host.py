@@ -13,7 +13,8 @@ from ionsolver_gb300 import workloads as W
 def test_stencil_kernel_names():
     cfg = dict(velocity_set=2, n_x=128)
     assert bench.stencil_kernel(cfg) == "k_sc_rows_ws"
-    assert bench.stencil_kernel(dict(cfg, n_x=384)) == "k_sc_rows"
+    assert bench.stencil_kernel(dict(cfg, n_x=384)) == "k_sc_rows_ws"
+    assert bench.stencil_kernel(dict(cfg, n_x=400)) == "k_sc_rows"
     assert bench.stencil_kernel(dict(cfg, n_x=24)) == "k_stream_collide"
     assert bench.stencil_kernel(dict(cfg, ext_subgrid_ecr=1)) == "k_stream_collide"
     assert bench.stencil_kernel(dict(cfg, velocity_set=1)) == "k_stream_collide"

@@ -166,17 +166,35 @@ def test_mhd_strict_bitwise_before_nan_onset_and_charge_conservation():
 def test_codecs_exhaustive_against_oracle():
     import ionsolver_gb300 as I
     lib = O.oracle_lib("f32")
-    raw = np.arange(65536, dtype=np.uint16)
     rng = np.random.default_rng(3)
-    vals = np.concatenate([rng.uniform(-2.0, 2.0, 40000), rng.normal(0, 1e-3, 20000),
-                           np.ldexp(rng.uniform(-1, 1, 5536), rng.integers(-30, 2, 5536))]).astype(np.float32)
-    for ft, enc_f, dec_f in ((0, lib.orc_fp16s_encode, lib.orc_fp16s_decode), (1, lib.orc_fp16c_encode, lib.orc_fp16c_decode)):
-        enc, dec, rdec = I.codec_roundtrip(ft, vals, raw)
-        e_ref = np.array([enc_f(float(v)) for v in vals], np.uint16)
-        d_ref = np.array([dec_f(int(r)) for r in raw], np.float32)
-        assert np.array_equal(enc, e_ref)
-        finite = np.isfinite(d_ref)
-        assert np.array_equal(rdec[finite].view(np.uint32), d_ref[finite].view(np.uint32))
+    # every float exponent from 2^-35 to 2^9 with the mantissas where the FP16C encoder's
+    # rounding carries or its normal/subnormal/zero cases switch, both signs; +-0, +-inf
+    # and NaNs (encoded as the canonical NaN, the oracle's GPU NaN model)
+    mant = np.array([0, 1, 0x7FF, 0x800, 0x801, 0xFFF, 0x1000, 0x3FF800, 0x7FF7FF, 0x7FF800, 0x7FFFFF], np.uint32)
+    exps = np.arange(92, 137, dtype=np.uint32)
+    edge = ((exps[:, None] << 23) | mant[None, :]).ravel()
+    special = np.array([0, 0x7F800000, 0x7FC00000, 0x7F800001, 0x7FFFFFFF], np.uint32)
+    bits = np.concatenate([edge, edge | 0x80000000, special, special | 0x80000000])
+    vals = np.concatenate([np.concatenate([rng.uniform(-2.0, 2.0, 40000), rng.normal(0, 1e-3, 20000),
+                                           np.ldexp(rng.uniform(-1, 1, 5536), rng.integers(-30, 2, 5536))]
+                                          ).astype(np.float32),
+                           bits.view(np.float32)])  # the bit patterns as they are (no cast)
+    raw = (np.arange(vals.size) % 65536).astype(np.uint16)  # every 16-bit pattern (and some twice)
+    lib.orc_set_nan_model(1)
+    try:
+        for ft, enc_f, dec_f in ((0, lib.orc_fp16s_encode, lib.orc_fp16s_decode),
+                                 (1, lib.orc_fp16c_encode, lib.orc_fp16c_decode)):
+            enc, dec, rdec = I.codec_roundtrip(ft, vals, raw)
+            e_ref = np.array([enc_f(float(v)) for v in vals], np.uint16)
+            d_ref = np.array([dec_f(int(r)) for r in raw[:65536]], np.float32)
+            rdec = rdec[:65536]
+            # FP16S: IEEE half of 2^15 x (a NaN's payload is not part of the format)
+            keep = ~np.isnan(vals) if ft == 0 else np.ones(len(vals), bool)
+            assert np.array_equal(enc[keep], e_ref[keep])
+            finite = np.isfinite(d_ref)
+            assert np.array_equal(rdec[finite].view(np.uint32), d_ref[finite].view(np.uint32))
+    finally:
+        lib.orc_set_nan_model(0)
 
 
 def test_shared_division_matches_ieee():
@@ -215,11 +233,13 @@ def test_subgrid_ecr_bitwise(ft, rt):
     assert U.compare_bitwise(g, o, names) == {n: 0 for n in names}
 
 
+@pytest.mark.parametrize("nx", [272, 400])
 @pytest.mark.parametrize("ft,rt", [(2, 0), (0, 0), (1, 1)], ids=["FP32-SRT", "FP16S-SRT", "FP16C-TRT"])
-def test_long_rows_bitwise(ft, rt):
-    """Rows longer than 256 cells take the other row-staged stream_collide form:
-    an elongated MHD box (272 x 16 x 16) bit-identical to the oracle after 2 steps."""
-    case = W.mhd_box(shape=(272, 16, 16), depth=2, magnet_r=5.0, magnet_t=3.0, float_type=ft)
+def test_long_rows_bitwise(ft, rt, nx):
+    """Rows of 257-384 cells take the producer-warp form with the 384-cell row stride,
+    longer rows the CTA-barrier form: elongated MHD boxes (nx x 16 x 16) bit-identical
+    to the oracle after 2 steps."""
+    case = W.mhd_box(shape=(nx, 16, 16), depth=2, magnet_r=5.0, magnet_t=3.0, float_type=ft)
     case["config"]["relaxation_time"] = rt
     g = U.run_gpu(case, 2)
     o = orc_run(case, 2)
@@ -227,10 +247,11 @@ def test_long_rows_bitwise(ft, rt):
     assert all(v == 0 for v in diff.values()), diff
 
 
+@pytest.mark.parametrize("nx", [288, 400])
 @pytest.mark.parametrize("ft", [2, 0, 1], ids=["FP32", "FP16S", "FP16C"])
-def test_long_rows_plain_trt_bitwise(ft):
-    """The long-row form without MHD: a 288 x 8 x 8 Taylor-Green box, TRT, 20 steps."""
-    case = W.taylor_green(shape=(288, 8, 8), amplitude=0.05, float_type=ft, relaxation_time=1)
+def test_long_rows_plain_trt_bitwise(ft, nx):
+    """Both long-row forms without MHD: an nx x 8 x 8 Taylor-Green box, TRT, 20 steps."""
+    case = W.taylor_green(shape=(nx, 8, 8), amplitude=0.05, float_type=ft, relaxation_time=1)
     g = U.run_gpu(case, 20)
     o = orc_run(case, 20)
     assert U.compare_bitwise(g, o, ["fi", "rho", "u"]) == {"fi": 0, "rho": 0, "u": 0}
