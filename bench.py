@@ -66,10 +66,10 @@ sys.path.insert(0, str(ROOT))
 FLOP_PER_INTERACTION = 34  # one source's E and B: 34 FLOP + 1 sqrt (sim_kernels.cl:950-954)
 # kernel-time results of one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum per launch);
 # the summaries with the commands that produced them are in profiles/
-# (rings384: the rings288 capture of k_sc_rows scaled by the cell count, (384/288)^3; every
+# (rings384: the rings192 capture of k_sc_rows_ws scaled by the cell count, (384/192)^3; every
 # stream is read and written once per cell, so the traffic is proportional to the cells)
-NCU_TRAFFIC = {("tgv256", "k_sc_rows_ws"): 2.506631e9, ("mhd128", "k_sc_rows_ws"): 0.807230e9,
-               ("mhd128", "k_update_e_b_fast"): 63.815e6, ("rings384", "k_sc_rows"): 64 / 27 * 5.628695e9}
+NCU_TRAFFIC = {("tgv256", "k_sc_rows_ws"): 2.505911e9, ("mhd128", "k_sc_rows_ws"): 0.816344e9,
+               ("mhd128", "k_update_e_b_fast"): 63.815e6, ("rings384", "k_sc_rows_ws"): 8 * 1.627825e9}
 
 
 def stencil_kernel(cfg: dict) -> str:
@@ -639,7 +639,7 @@ def main():
             kname = "k_update_e_b_exact" if a.field_mode == "bitwise" else "k_update_e_b_fast"
         else:
             avg = ms / a.steps
-            kname = f"k_batch_step<{a.field_mode}> (whole step; FLOPs of its E/B phase)"
+            kname = f"k_batch_stream + k_batch_field<{a.field_mode}> (whole step; FLOPs of its E/B phase)"
         tflops = inter * FLOP_PER_INTERACTION / (avg * 1e-3) / 1e12
         roofline = {"bound": "fp32", "achieved": tflops, "peak": tf.value, "unit": "TFLOP/s",
                     "frac": tflops / tf.value, "traffic": NCU_TRAFFIC.get((a.workload, kname)), "kernel": kname,
