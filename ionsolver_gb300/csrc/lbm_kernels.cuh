@@ -1,5 +1,6 @@
 // lbm_kernels.cuh -- initialize / stream_collide / update_fields of the
-// IonSolver timestep as sm_103a kernels (one thread per cell, grid-stride).
+// IonSolver timestep as sm_103a kernels (one thread per cell: grid-stride over
+// the cells, or over x-rows staged in shared memory for D3Q19 stream_collide).
 //
 // Per cell the arithmetic follows the reference kernel operation for
 // operation (IonSolver src/kernels/sim_kernels.cl:465-859), so results are

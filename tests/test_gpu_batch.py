@@ -19,7 +19,8 @@ def _cases_mhd(ft, fm):
     return out
 
 
-@pytest.mark.parametrize("ft,fm", [(2, 0), (2, 1), (0, 1)], ids=["FP32-bitwise", "FP32-fast", "FP16S-fast"])
+@pytest.mark.parametrize("ft,fm", [(2, 0), (2, 1), (0, 1), (1, 1)], ids=["FP32-bitwise", "FP32-fast", "FP16S-fast",
+                                                                       "FP16C-fast"])
 def test_batch_equals_individual_mhd(ft, fm):
     cases = _cases_mhd(ft, fm)
     steps = 26
