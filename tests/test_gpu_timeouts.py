@@ -26,7 +26,7 @@ def _reset(lbm, case):
     lbm.initialize()
 
 
-@pytest.mark.parametrize("nx", [32, 272], ids=["producer-warp-rows", "long-rows"])
+@pytest.mark.parametrize("nx", [32, 272, 400], ids=["producer-warp-rows", "producer-warp-384-rows", "long-rows"])
 def test_single_domain_wait_expires_and_recovers(nx):
     case = W.mhd_plasma(shape=(nx, 16, 16), depth=2, magnet_r=4.0, magnet_t=3.0, field_mode=1)
     g = U.setup_gpu(case)
