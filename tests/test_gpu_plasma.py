@@ -26,7 +26,7 @@ from tests import _util as U
 
 pytestmark = pytest.mark.gpu
 
-# Per-cell bound of the FAST field against BITWISE (the benchmark spec: <= 1e-4 in FP32),
+# Per-cell bound of the FAST field against BITWISE (the target: <= 1e-4 in FP32),
 # vector norms per cell: |dF_cell| / max(|F_cell|, FLOOR * max_cells |F_cell|).  The
 # floor keeps cells where the sum of thousands of +-q/r^2 terms nearly cancels from
 # dividing by a residue.  F is E_dyn and B_dyn, the fields the next step uses; their
