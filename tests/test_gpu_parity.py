@@ -257,6 +257,22 @@ def test_long_rows_plain_trt_bitwise(ft, nx):
     assert U.compare_bitwise(g, o, ["fi", "rho", "u"]) == {"fi": 0, "rho": 0, "u": 0}
 
 
+@pytest.mark.parametrize("nx", [16, 144, 240, 368])
+def test_row_strides_bitwise(nx):
+    """Rows that fill the shared-memory row stride only partly (128-element stride: 16
+    cells; 256: 144, 240; 384: 368): an MHD box in FP16C (the written-back rows, the
+    shared two-pass code) and a plain FP16S TRT box, bit-identical to the oracle."""
+    case = W.mhd_box(shape=(nx, 16, 8), depth=2, magnet_r=3.0, magnet_t=2.0, float_type=1)
+    g = U.run_gpu(case, 2)
+    o = orc_run(case, 2)
+    diff = U.compare_bitwise(g, o, U.field_names(case))
+    assert all(v == 0 for v in diff.values()), diff
+    case = W.taylor_green(shape=(nx, 8, 4), amplitude=0.05, float_type=0, relaxation_time=1)
+    g = U.run_gpu(case, 10)
+    o = orc_run(case, 10)
+    assert U.compare_bitwise(g, o, ["fi", "rho", "u"]) == {"fi": 0, "rho": 0, "u": 0}
+
+
 @pytest.mark.parametrize("ft", [2, 0, 1], ids=["FP32", "FP16S", "FP16C"])
 def test_mhd_trt_bitwise(ft):
     """MHD with TRT collision through the row-staged stream_collide (32^3, depth 4)."""
