@@ -1229,6 +1229,8 @@ struct ion_batch {
     uint32_t total_bricks[3] = {0, 0, 0};
     uint32_t* d_bin_off = nullptr;
     uint32_t total_bins = 0;
+    uint32_t* d_row_off = nullptr;  // row-staged stencil: prefix sums of ny nz (null: tiles of cells)
+    uint32_t total_rows = 0;
     uint32_t* d_sync = nullptr;  // [0] barrier count, [1] barrier generation, [2] error
     uint32_t barrier_limit = BARRIER_LIMIT;
     uint64_t t = 0;
@@ -1262,6 +1264,8 @@ BatchDev batch_view(ion_batch* b, uint32_t block) {
     B.bar_gen = b->d_sync + 1;
     B.err = b->d_sync + 2;
     B.barrier_limit = b->barrier_limit;
+    B.row_off = b->d_row_off;
+    B.total_rows = b->total_rows;
     return B;
 }
 
@@ -1357,6 +1361,21 @@ int ion_batch_create(ion_lbm* const* domains, uint32_t count, ion_batch** out) {
         if (!rc && cudaMemcpy(b->d_brick_off[s], bricks.data(), sizeof(uint32_t) * (count + 1), cudaMemcpyHostToDevice) != cudaSuccess)
             rc = fail(ION_E_CUDA, "batch table upload");
     }
+    // the row-staged stencil when every domain's rows are whole 16-byte streams of at most
+    // BATCH_ROW_MAX cells and its slot offsets fit in 32 bits (as for k_sc_rows_ws)
+    bool rows_ok = true;
+    std::vector<uint32_t> rows(count + 1, 0);
+    for (uint32_t i = 0; i < count; i++) {
+        const DevLbm& L = domains[i]->L;
+        rows_ok = rows_ok && L.nx % 16u == 0u && L.nx <= BATCH_ROW_MAX && 19ull * L.n < (1ull << 32);
+        rows[i + 1] = rows[i] + L.ny * L.nz;
+    }
+    if (!rc && rows_ok) {
+        b->total_rows = rows[count];
+        rc = dalloc((void**)&b->d_row_off, sizeof(uint32_t) * (count + 1));
+        if (!rc && cudaMemcpy(b->d_row_off, rows.data(), sizeof(uint32_t) * (count + 1), cudaMemcpyHostToDevice) != cudaSuccess)
+            rc = fail(ION_E_CUDA, "batch table upload");
+    }
     if (!rc && (cudaMemcpy(b->d_doms, views.data(), sizeof(DevLbm) * count, cudaMemcpyHostToDevice) != cudaSuccess ||
                 cudaMemcpy(b->d_bin_off, bins.data(), sizeof(uint32_t) * (count + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
                 cudaMemset(b->d_sync, 0, sizeof(uint32_t) * 4) != cudaSuccess))
@@ -1379,7 +1398,7 @@ int ion_batch_destroy(ion_batch* b) {
 static int batch_autotune(ion_batch* b, uint64_t& steps) {
     float best = 1e30f;
     for (uint32_t block : kBatchBlocks) {
-        const int maxb = batch_max_blocks_per_sm(b->ft, b->mhd, b->fast, (int)block);
+        const int maxb = batch_max_blocks_per_sm(b->ft, b->mhd, b->fast, b->total_rows > 0u, (int)block);
         for (int bps = 1; bps <= std::min(maxb, 4); bps++) {
             if (steps < 2) break;
             const uint32_t grid = (uint32_t)(bps * b->sms);
@@ -1398,7 +1417,8 @@ static int batch_autotune(ion_batch* b, uint64_t& steps) {
     }
     if (b->grid == 0) {  // not enough steps to tune: the middle shape
         b->block = 256;
-        b->grid = (uint32_t)(std::max(1, std::min(2, batch_max_blocks_per_sm(b->ft, b->mhd, b->fast, 256))) * b->sms);
+        b->grid = (uint32_t)(std::max(1, std::min(2, batch_max_blocks_per_sm(b->ft, b->mhd, b->fast, b->total_rows > 0u, 256))) *
+                             b->sms);
     } else {
         b->tuned = true;
     }

@@ -52,10 +52,15 @@ struct BatchDev {
     uint32_t* bar_gen;
     uint32_t* err;
     uint32_t barrier_limit;  // polls before a grid barrier gives up
+    const uint32_t* row_off;   // [ndom+1] prefix sums of ny nz (the row-staged stencil), or null
+    uint32_t total_rows;       // 0: the stencil runs in tiles of cells with global loads
 };
-// threads per block of the batch's stencil kernel (its tiles: BATCH_SC_THREADS * EB_CPT cells)
+// threads per block of the batch's stencil kernel (its tiles: BATCH_SC_THREADS * EB_CPT cells;
+// row-staged: BATCH_SC_THREADS - 32 compute threads, so rows of up to BATCH_ROW_MAX cells,
+// staged at a row stride of BATCH_ROW_STRIDE elements)
 constexpr uint32_t BATCH_SC_THREADS = 128;
-int batch_max_blocks_per_sm(int ft, bool mhd, bool fast, int block);
+constexpr uint32_t BATCH_ROW_MAX = BATCH_SC_THREADS - 32, BATCH_ROW_STRIDE = 128;
+int batch_max_blocks_per_sm(int ft, bool mhd, bool fast, bool rows, int block);
 cudaError_t launch_batch_step(const BatchDev& B, int ft, bool mhd, bool fast, uint32_t grid, uint32_t block,
                               uint64_t t, cudaStream_t s);
 
