@@ -639,7 +639,8 @@ def main():
             kname = "k_update_e_b_exact" if a.field_mode == "bitwise" else "k_update_e_b_fast"
         else:
             avg = ms / a.steps
-            kname = f"k_batch_stream + k_batch_field<{a.field_mode}> (whole step; FLOPs of its E/B phase)"
+            kname = (f"k_batch_stream{'_rows' if all(c['config']['n_x'] % 16 == 0 and c['config']['n_x'] <= 96 for c in cases) else ''}"
+                     f" + k_batch_field<{a.field_mode}> (whole step; FLOPs of its E/B phase)")
         tflops = inter * FLOP_PER_INTERACTION / (avg * 1e-3) / 1e12
         roofline = {"bound": "fp32", "achieved": tflops, "peak": tf.value, "unit": "TFLOP/s",
                     "frac": tflops / tf.value, "traffic": NCU_TRAFFIC.get((a.workload, kname)), "kernel": kname,
