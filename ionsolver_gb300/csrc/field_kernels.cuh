@@ -411,6 +411,11 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t brick, c
     const float ox = (float)(bx * EB_BX) + 0.5f * (float)(EB_BX - 1);
     const float oy = (float)(by * EB_BY) + 0.5f * (float)(EB_BY - 1);
     const float oz = (float)(bz * EB_CPT) + 0.5f * (float)(EB_CPT - 1);
+    // depth-D LOD bins [first_src, n_lod_own) except the cell's own (sim_kernels.cl:940-955);
+    // the first chunk's copy starts now, so it lands while the near field is summed
+    const uint32_t first = L.first_src, last = src_last<FAST>(L);
+    const uint32_t nchunks = (last - first + SRC_CHUNK - 1u) / SRC_CHUNK;
+    if (threadIdx.x == 0 && nchunks > 0) eb_issue(L, sm, 0, last);
     float e[EB_CPT][3], b[EB_CPT][3];  // near field (and, BITWISE, everything)
     float ax[EB_CPT], ay[EB_CPT], az[EB_CPT];  // BITWISE: absolute coordinates
     float rx[EB_CPT], ry[EB_CPT], rz[EB_CPT];  // FAST: coordinates relative to the brick centre
@@ -451,7 +456,6 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t brick, c
         // The box's bins are staged in shared memory (sm.fast is free until the far loop)
         // in batches of NEAR_BATCH; every thread then sums them for its cells, the pair
         // (2j, 2j+1) -- the same x and y, z one apart -- in packed instructions.
-        const uint32_t first = L.first_src, last = src_last<FAST>(L);
         const uint32_t ex = box_hi[0] - box_lo[0] + 1u, ey = box_hi[1] - box_lo[1] + 1u;
         const uint32_t nbox = ex * ey * (box_hi[2] - box_lo[2] + 1u);
         float4* stage = reinterpret_cast<float4*>(sm.fast);  // [NEAR_BATCH] centres + index, then (q, q v)
@@ -502,10 +506,6 @@ __device__ __forceinline__ bool eb_tile(const DevLbm& L, const uint32_t brick, c
         far_zero(fs[j]);
     }
 
-    // depth-D LOD bins [first_src, n_lod_own) except the cell's own (sim_kernels.cl:940-955)
-    const uint32_t first = L.first_src, last = src_last<FAST>(L);
-    const uint32_t nchunks = (last - first + SRC_CHUNK - 1u) / SRC_CHUNK;
-    if (threadIdx.x == 0 && nchunks > 0) eb_issue(L, sm, 0, last);
     bool ok = true;
     uint32_t c = 0;
     for (; c < nchunks; c++) {
