@@ -16,7 +16,8 @@ Workloads (``--workload``; default ``mhd128``, the headline configuration):
       fallbacks) against the exact FP32 step of the same box.
   batch96 : 96 independent MHD domains, cube edges from {32,48,64,80,96}
       (seed 3), a disk magnet each (radius 4..12, seed 4), one persistent
-      launch per step for all of them, autotuned launch shape, CUDA graph.
+      launch per step for all of them, autotuned launch shape, CUDA graph
+      (batch16: 16 such domains, a case small enough for a full ncu capture).
   rings384 : 384^3, FP16S storage, two coaxial ring magnets (R_out 48, R_in 32,
       t 12, centres 128 apart, axis z; rings192 and rings288 the same at 1/2 and
       3/4 scale, for profiling), LOD depth 4, the learned far field
@@ -88,7 +89,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="mhd128",
-                   choices=["mhd128", "mhd256", "mhd64", "batch96", "rings384", "rings192", "rings192d3", "rings288", "tgv64",
+                   choices=["mhd128", "mhd256", "mhd64", "batch96", "batch16", "rings384", "rings192", "rings192d3", "rings288", "tgv64",
                             "tgv256", "tgv384"])
     p.add_argument("--field-mode", default=None, choices=["bitwise", "fast", "surrogate"],
                    help="default: surrogate for rings384, fast otherwise")
@@ -124,8 +125,8 @@ def make_cases(a) -> list[dict]:
     ft = FT[a.float_type]
     w = a.workload
     plasma = a.start == "plasma"
-    if w == "batch96":
-        return W.batch_domains(96, float_type=ft, field_mode=fm, plasma=plasma)
+    if w.startswith("batch"):  # batch16: 16 domains drawn as batch96's are (a profiling case)
+        return W.batch_domains(int(w[5:]), float_type=ft, field_mode=fm, plasma=plasma)
     if w.startswith("rings"):  # rings192: the same box at half the size; rings192d3: LOD depth 3, i.e. the
         n, _, d = w[5:].partition("d")  # 24^3-cell bins of rings384 (profiling cases)
         case = W.mhd_box(n=int(n), float_type=ft, depth=int(d or 4), field_mode=fm, rings=True)
