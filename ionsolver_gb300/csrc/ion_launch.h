@@ -57,9 +57,11 @@ struct BatchDev {
 };
 // threads per block of the batch's stencil kernel (its tiles: BATCH_SC_THREADS * EB_CPT cells;
 // row-staged: BATCH_SC_THREADS - 32 compute threads, so rows of up to BATCH_ROW_MAX cells,
-// staged at a row stride of BATCH_ROW_STRIDE elements)
+// staged at a row stride of BATCH_ROW_STRIDE elements: 96 x 4 bytes keeps every stream
+// 16-byte aligned, and the smaller buffers fit five CTAs per SM in FP32 MHD)
 constexpr uint32_t BATCH_SC_THREADS = 128;
-constexpr uint32_t BATCH_ROW_MAX = BATCH_SC_THREADS - 32, BATCH_ROW_STRIDE = 128;
+constexpr uint32_t BATCH_ROW_MAX = BATCH_SC_THREADS - 32, BATCH_ROW_STRIDE = BATCH_ROW_MAX;
+static_assert(BATCH_ROW_STRIDE % 16 == 0, "row streams of 16-byte multiples in shared memory");
 int batch_max_blocks_per_sm(int ft, bool mhd, bool fast, bool rows, int block);
 cudaError_t launch_batch_step(const BatchDev& B, int ft, bool mhd, bool fast, uint32_t grid, uint32_t block,
                               uint64_t t, cudaStream_t s);
