@@ -62,6 +62,28 @@ def test_boundaries_and_forces_bitwise(rt, nx):
     assert U.compare_bitwise(g, o, ["fi", "rho", "u", "flags"]) == {"fi": 0, "rho": 0, "u": 0, "flags": 0}
 
 
+@pytest.mark.parametrize("nx", [24, 32], ids=["global-loads", "row-staged"])
+@pytest.mark.parametrize("ft", [2, 1], ids=["FP32", "FP16C"])
+def test_mhd_boundaries_and_forces_bitwise(ft, nx):
+    """MHD with equilibrium (inflow) cells, an obstacle and a force field on the
+    finite-plasma start: the electron gas, the gas and the charge lattice at the
+    equilibrium cells (sim_kernels.cl:651-655), 30 steps, every field bit-identical."""
+    ny, nz = 20, 16
+    N = nx * ny * nz
+    rng = np.random.default_rng(27)
+    case = W.mhd_plasma(shape=(nx, ny, nz), float_type=ft, depth=2, magnet_r=4.0, magnet_t=3.0, field_mode=0)
+    flags = W.shell_flags(nx, ny, nz)
+    flags.reshape(nz, ny, nx)[:, :, 0] = 0x02      # equilibrium inlet plane
+    flags.reshape(nz, ny, nx)[8:11, 5:9, 14:18] = 0x01  # an obstacle
+    case["fields"].update(flags=flags, F=rng.normal(0, 1e-5, 3 * N).astype(np.float32),
+                          rho=(1.0 + rng.normal(0, 1e-3, N)).astype(np.float32))
+    case["config"].update(ext_equilibrium_boundaries=1, ext_force_field=1, f_x=1e-6, f_y=-2e-6, f_z=5e-7)
+    g = U.run_gpu(case, 30)
+    o = orc_run(case, 30)
+    diff = U.compare_bitwise(g, o, U.field_names(case))
+    assert all(v == 0 for v in diff.values()), diff
+
+
 @pytest.mark.parametrize("ft", [2, 0, 1], ids=["FP32", "FP16S", "FP16C"])
 @pytest.mark.parametrize("n,depth,r,t", [(32, 4, 6.0, 4.0), (16, 2, 4.0, 3.0), (24, 3, 5.0, 4.0)],
                          ids=["32c-D4", "16c-D2", "24c-D3"])

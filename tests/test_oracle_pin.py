@@ -61,6 +61,27 @@ def test_boundaries_and_forces(rt):
     assert_same(a, b, ["fi", "rho", "u", "flags"])
 
 
+@pytest.mark.parametrize("ft", [2, 1], ids=["FP32", "FP16C"])
+def test_mhd_boundaries_and_forces(ft):
+    """MHD with equilibrium (inflow) cells, an obstacle and a force field, on the
+    finite-plasma start: the electron gas, the gas and the charge lattice at the
+    equilibrium cells (sim_kernels.cl:651-655), 30 steps, every field finite."""
+    nx, ny, nz = 12, 10, 8
+    N = nx * ny * nz
+    rng = np.random.default_rng(17)
+    case = W.mhd_plasma(shape=(nx, ny, nz), float_type=ft, depth=1, magnet_r=2.0, magnet_t=2.0)
+    flags = W.shell_flags(nx, ny, nz)
+    flags.reshape(nz, ny, nx)[:, :, 0] = 0x02
+    flags.reshape(nz, ny, nx)[3:5, 3:6, 6:8] = 0x01
+    case["fields"].update(flags=flags, F=rng.normal(0, 1e-5, 3 * N).astype(np.float32),
+                          rho=(1.0 + rng.normal(0, 1e-3, N)).astype(np.float32))
+    case["config"].update(ext_equilibrium_boundaries=1, ext_force_field=1, f_x=1e-6, f_y=-2e-6, f_z=5e-7)
+    a, b = run_both(case, 30)
+    assert_same(a, b, U.field_names(case))
+    for n in ("rho", "u", "q", "e_dyn", "b_dyn"):
+        assert np.isfinite(a.field(n)).all(), n
+
+
 @pytest.mark.parametrize("ft,n,depth,uf", [(2, 16, 2, 1), (0, 16, 2, 1), (1, 16, 2, 1), (2, 16, 4, 1), (2, 8, 1, 0),
                                            (2, 16, 0, 1), (2, 16, 3, 1)],
                          ids=["FP32-D2", "FP16S-D2", "FP16C-D2", "FP32-D4", "FP32-D1-noUF", "FP32-D0", "FP32-D3"])
