@@ -95,6 +95,29 @@ def test_mhd_bitwise(ft, n, depth, r, t):
     assert all(v == 0 for v in diff.values()), diff
 
 
+@pytest.mark.parametrize("nx", [24, 32], ids=["global-loads", "row-staged"])
+def test_mhd_without_field_output_bitwise(nx):
+    """update_fields off (rho and u are not written by stream_collide) with MHD on the
+    finite-plasma start, LOD depth 1: every other field bit-identical after 20 steps."""
+    case = W.mhd_plasma(shape=(nx, 16, 16), depth=1, magnet_r=4.0, magnet_t=3.0, field_mode=0, update_fields=0)
+    g = U.run_gpu(case, 20)
+    o = orc_run(case, 20)
+    diff = U.compare_bitwise(g, o, U.field_names(case))
+    assert all(v == 0 for v in diff.values()), diff
+
+
+@pytest.mark.parametrize("ft", [2, 0, 1], ids=["FP32", "FP16S", "FP16C"])
+def test_mhd_d3q15_bitwise(ft):
+    """MHD on the D3Q15 velocity set (the global-load stream_collide), finite-plasma
+    start, 20 steps, every field bit-identical."""
+    case = W.mhd_plasma(shape=(16, 16, 16), float_type=ft, depth=2, magnet_r=4.0, magnet_t=3.0, field_mode=0)
+    case["config"]["velocity_set"] = 1
+    g = U.run_gpu(case, 20)
+    o = orc_run(case, 20)
+    diff = U.compare_bitwise(g, o, U.field_names(case))
+    assert all(v == 0 for v in diff.values()), diff
+
+
 def test_mhd_fast_field_close():
     """FAST field mode: same sources and order, rsqrt/FMA arithmetic."""
     case = W.mhd_box(n=32, depth=4, magnet_r=6.0, magnet_t=4.0, field_mode=1)

@@ -105,6 +105,18 @@ def test_mhd_finite_plasma(ft, rt):
         assert np.isfinite(a.field(n)).all(), n
 
 
+@pytest.mark.parametrize("ft", [2, 0], ids=["FP32", "FP16S"])
+def test_mhd_d3q15_finite_plasma(ft):
+    """MHD on the D3Q15 velocity set (electron gas and gas lattices D3Q15, charge D3Q7),
+    finite-plasma start: 20 steps bit for bit, every field finite."""
+    case = W.mhd_plasma(shape=(16, 16, 16), float_type=ft, depth=2, magnet_r=4.0, magnet_t=3.0)
+    case["config"]["velocity_set"] = 1
+    a, b = run_both(case, 20)
+    assert_same(a, b, U.field_names(case))
+    for n in ("rho", "u", "q", "e_dyn", "b_dyn"):
+        assert np.isfinite(a.field(n)).all(), n
+
+
 def test_mhd_trt():
     case = W.mhd_box(n=16, depth=2, magnet_r=4.0, magnet_t=3.0)
     case["config"]["relaxation_time"] = 1
