@@ -118,6 +118,17 @@ def test_mhd_d3q15_bitwise(ft):
     assert all(v == 0 for v in diff.values()), diff
 
 
+@pytest.mark.parametrize("depth", [0, 1])
+def test_mhd_shallow_lod_bitwise(depth):
+    """LOD depth 0 (no bins: the field is the static one) and 1 (8 bins), finite-plasma
+    start, the row-staged stencil: every field bit-identical to the oracle after 20 steps."""
+    case = W.mhd_plasma(shape=(32, 16, 16), depth=depth, magnet_r=4.0, magnet_t=3.0, field_mode=0)
+    g = U.run_gpu(case, 20)
+    o = orc_run(case, 20)
+    diff = U.compare_bitwise(g, o, U.field_names(case))
+    assert all(v == 0 for v in diff.values()), diff
+
+
 def test_mhd_fast_field_close():
     """FAST field mode: same sources and order, rsqrt/FMA arithmetic."""
     case = W.mhd_box(n=32, depth=4, magnet_r=6.0, magnet_t=4.0, field_mode=1)
