@@ -103,6 +103,9 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--start", default="plasma", choices=["plasma", "reference"],
                    help="initial electron gas of the MHD workloads (see the module docstring)")
+    p.add_argument("--update-fields", default=None, choices=["on", "off"],
+                   help="rho/u written by every stream_collide (default: on for MHD, as the reference with its "
+                        "graphics active; off for the plain TGV boxes)")
     p.add_argument("--no-surrogate-record", action="store_true",
                    help="mhd128: leave out the learned-far-field record (rings384)")
     p.add_argument("--surrogate-size", type=int, default=384, help="box edge of the mhd128 line's surrogate record")
@@ -120,6 +123,14 @@ FM = {"bitwise": 0, "fast": 1, "surrogate": 2}
 
 
 def make_cases(a) -> list[dict]:
+    cases = _make_cases(a)
+    if getattr(a, "update_fields", None) is not None:
+        for c in cases:
+            c["config"]["update_fields"] = int(a.update_fields == "on")
+    return cases
+
+
+def _make_cases(a) -> list[dict]:
     from ionsolver_gb300 import workloads as W
     fm = FM[a.field_mode]
     ft = FT[a.float_type]

@@ -39,6 +39,17 @@ def test_workload_names(monkeypatch):
     assert (seen[1]["n"], seen[1]["depth"]) == (384, 4)
 
 
+def test_update_fields_option():
+    """--update-fields on/off overrides the workloads' default (on for MHD, off for TGV)."""
+    a = types.SimpleNamespace(field_mode="fast", float_type="FP32", workload="mhd64", start="plasma")
+    assert bench.make_cases(a)[0]["config"]["update_fields"] == 1
+    a.update_fields = "off"
+    c = bench.make_cases(a)[0]["config"]
+    assert c["update_fields"] == 0 and bench.bytes_per_lup(c) == bench.bytes_per_lup(dict(c, update_fields=1)) - 16
+    a = types.SimpleNamespace(field_mode="fast", float_type="FP32", workload="tgv64", start="plasma", update_fields="on")
+    assert bench.make_cases(a)[0]["config"]["update_fields"] == 1
+
+
 def test_plasma_start_cases():
     """--start plasma: the same geometry and seeds, plasma units, the electron background."""
     a = types.SimpleNamespace(field_mode="fast", float_type="FP32", workload="mhd64", start="plasma")
